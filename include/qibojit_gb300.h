@@ -1,0 +1,141 @@
+/*
+ * qibojit_gb300.h -- C ABI of the GB300 state-vector engine.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (SV_OK = 0).  State vectors, probability and frequency arrays are DEVICE
+ * pointers owned by the caller (torch, cupy or cudaMalloc'd memory); the engine
+ * mutates states in place and never frees caller memory.  Gate operands (2x2,
+ * 4x4, 2^k x 2^k row-major matrices, the U1 phase scalar, the 5-entry fSim
+ * vector) and qubit lists are HOST pointers, read before the call returns.
+ * Work is enqueued on the context's stream and is asynchronous unless the entry
+ * point says otherwise; sv_sync() waits for it.
+ *
+ * Conventions (qibojit src/qibojit/backends/cpu.py:565-635):
+ *   - qubit q of an n-qubit state is bit n-q-1 of the amplitude index;
+ *   - `qubits` lists (the reference's "qubits tensor") are the SORTED bit
+ *     positions n-q-1 of all controls and targets of a gate, int32;
+ *   - a two-target gate's row index is 2*bit(target1) + bit(target2) in the
+ *     order the targets are given; a k-target gate's row index has target[0]
+ *     as its most significant bit.
+ *
+ * Status codes map to the reference's Python exceptions in the Python layer:
+ * SV_ERR_ARG -> ValueError, SV_ERR_OOM -> RuntimeError (gpu.py:733-739),
+ * SV_ERR_NO_DEVICE -> ImportError (gpu.py:85-91), others -> RuntimeError.
+ */
+#ifndef QIBOJIT_GB300_H
+#define QIBOJIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum sv_status {
+  SV_OK = 0,
+  SV_ERR_ARG = 1,         /* bad argument (qubit out of range, duplicate qubit, k too large) */
+  SV_ERR_OOM = 2,         /* device allocation failed */
+  SV_ERR_CUDA = 3,        /* CUDA runtime error */
+  SV_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  SV_ERR_UNSUPPORTED = 5, /* kernel/dtype combination not supported (e.g. Y on a real state) */
+  SV_ERR_NO_DEVICE = 6    /* no usable CUDA device */
+};
+
+/* Amplitude types, as CupyBackend compiles its kernels for (gpu.py:107-112). */
+enum sv_dtype { SV_C128 = 0, SV_C64 = 1, SV_F64 = 2, SV_F32 = 3 };
+
+/* One-target kernel families, GATE_OPS (cpu.py:23-36) plus the default "apply_gate". */
+enum sv_one_kind { SV_APPLY_GATE = 0, SV_APPLY_X = 1, SV_APPLY_Y = 2, SV_APPLY_Z = 3, SV_APPLY_Z_POW = 4 };
+/* Two-target kernel families (cpu.py:23-36) plus the default "apply_two_qubit_gate". */
+enum sv_two_kind { SV_APPLY_TWO_QUBIT_GATE = 0, SV_APPLY_SWAP = 1, SV_APPLY_FSIM = 2 };
+
+typedef struct sv_context sv_context;
+
+/* ---------------------------------------------------------------- context */
+/* Library version (major*10000 + minor*100 + patch). */
+int sv_version(void);
+/* Message of the last failed call on this host thread ("" if none). */
+const char* sv_last_error(void);
+/* Number of CUDA devices visible, or -1 if the runtime cannot be queried. */
+int sv_device_count(void);
+/* Creates an engine context on `device` (CupyBackend.__init__, gpu.py:50-143,
+ * without the runtime compilation: kernels are prebuilt for sm_103a). */
+int sv_context_create(int device, sv_context** out);
+int sv_context_destroy(sv_context* ctx);
+/* Sets the cudaStream_t (as void*) later calls enqueue on; NULL = legacy default stream. */
+int sv_context_set_stream(sv_context* ctx, void* stream);
+/* Blocks until all work enqueued on the context's stream is done (the reference's
+ * stream.synchronize() after each kernel, gpu.py:598, 638, 1006, 1035, 1075). */
+int sv_sync(sv_context* ctx);
+
+/* ---------------------------------------------------------- state creation */
+/* |0...0>: state[0] = 1, all others 0.  Replaces ops.initial_state_vector
+ * (custom_operators/ops.py:10-18) / CupyBackend.zero_state (gpu.py:584-600). */
+int sv_zero_state(sv_context* ctx, void* state, int dtype, int nqubits);
+
+/* ------------------------------------------------------------ gate kernels */
+/* One target, any number of controls.  Replaces NumbaBackend._one_qubit_base
+ * (cpu.py:606-616) and CupyBackend._one_qubit_base (gpu.py:1009-1036), i.e. the
+ * {multicontrol_}apply_{gate,x,y,z,z_pow}_kernel family (gates.py:15-114).
+ * gate: 4 values (2x2 row-major) for SV_APPLY_GATE, 1 value (the U1 phase) for
+ * SV_APPLY_Z_POW, ignored (may be NULL) otherwise; same dtype as the state.
+ * qubits: sorted bit positions of controls and target (nq = ncontrols + 1), or
+ * NULL / nq = 0 for an uncontrolled gate. */
+int sv_apply_one_qubit(sv_context* ctx, void* state, int dtype, int nqubits, int kind,
+                       const void* gate, int target, const int32_t* qubits, int nq);
+
+/* Two targets, any number of controls.  Replaces _two_qubit_base (cpu.py:618-635,
+ * gpu.py:1038-1076): {multicontrol_}apply_{two_qubit_gate,swap,fsim}_kernel
+ * (gates.py:117-254).  gate: 16 values for SV_APPLY_TWO_QUBIT_GATE, the 5-entry
+ * fSim operand (matrices.py:62-70) for SV_APPLY_FSIM, ignored for SV_APPLY_SWAP.
+ * qubits: as above with nq = ncontrols + 2, or NULL / 0. */
+int sv_apply_two_qubit(sv_context* ctx, void* state, int dtype, int nqubits, int kind,
+                       const void* gate, int target1, int target2, const int32_t* qubits, int nq);
+
+/* k = ntargets targets (1 <= k <= 10), any number of controls.  Replaces
+ * _multi_qubit_base (cpu.py:581-604, gpu.py:975-1007) and the
+ * apply_{three,four,five,multi}_qubit_gate kernels (gates.py:265-424).
+ * targets: qubit indices in gate order; gate: 4^k values row-major.
+ * qubits: sorted bit positions of controls and targets, or NULL / 0. */
+int sv_apply_multi_qubit(sv_context* ctx, void* state, int dtype, int nqubits,
+                         const void* gate, const int32_t* targets, int ntargets,
+                         const int32_t* qubits, int nq);
+
+/* ---------------------------------------------------------------- collapse */
+/* Zeroes the amplitudes whose measured bits differ from `result` and, when
+ * `normalize`, divides the kept ones by their FP64 (compensated) norm.
+ * `qubits`: the measured qubit indices in the order given (the reference maps
+ * them to reversed bit positions, cpu.py:548-552); bit j of `result` (counting
+ * from the most significant) is the outcome of qubits[j].  Replaces
+ * NumbaBackend._collapse_statevector (cpu.py:541-563) -> ops.collapse_state /
+ * collapse_state_normalized (ops.py:43-79), and CupyBackend.collapse_state
+ * (gpu.py:616-644).  Uses context scratch for the norm partials. */
+int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits,
+                      const int32_t* qubits, int nq, int64_t result, int normalize);
+
+/* ----------------------------------------------------------- probabilities */
+/* out[o] = sum of |amp|^2 over amplitudes whose measured bits spell o, with
+ * qubits[0] the most significant bit of o (qibo Backend.calculate_probabilities,
+ * wrapped by CupyBackend at gpu.py:751-768).  Accumulates in FP64; out_dtype is
+ * SV_F64 or SV_F32 (rounded from the FP64 sums).  `out` has 2^nq entries. */
+int sv_probabilities(sv_context* ctx, const void* state, int dtype, int nqubits,
+                     const int32_t* qubits, int nq, void* out, int out_dtype);
+
+/* ------------------------------------------------------------- sampling */
+/* Metropolis sampling of `nshots` outcomes from `probs` (2^nbits entries,
+ * SV_F64 or SV_F32), `nchains` independent chains, accumulated into the int64
+ * device array `frequencies`.  Reproduces ops.measure_frequencies
+ * (ops.py:82-108) exactly: chain seeds are NumPy-legacy randint(0, 1e8) draws
+ * after seeding with `seed`; every chain starts at the first argmax of probs,
+ * proposes (shot + randint(0, N)) % N and accepts when
+ * probs[new] / probs[shot] > random(), with NumPy's legacy MT19937 streams. */
+int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* probs,
+                           int prob_dtype, int nbits, int64_t nshots, uint32_t seed,
+                           int nchains);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QIBOJIT_GB300_H */

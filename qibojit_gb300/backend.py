@@ -1,0 +1,357 @@
+"""``GB300Backend``: qibojit's backend API on the GB300 engine.
+
+The class mirrors the methods qibojit's ``NumbaBackend`` / ``CupyBackend`` expose
+for state vectors (``src/qibojit/backends/cpu.py:39-635``,
+``src/qibojit/backends/gpu.py:44-1076``): ``apply_gate`` and the
+``_one/_two/_multi_qubit_base`` kernels it dispatches to, ``zero_state``,
+``collapse_state``, ``calculate_probabilities``, ``sample_frequencies`` and
+``measure_frequencies_op``, plus the dtype/device/seed/thread setters.  Every
+amplitude operation is one call through the C ABI into the CUDA library; there is
+no CPU path.  Device arrays are torch CUDA tensors (any contiguous CUDA tensor of
+the backend's dtype works), used only as memory.
+"""
+from __future__ import annotations
+
+import os
+from collections import Counter
+from typing import List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _lib
+from .matrices import CustomMatrices, Matrices
+
+try:  # plug into qibo when it is installed
+    from qibo.backends import Backend as _QiboBackend  # type: ignore
+except Exception:  # pragma: no cover - qibo is optional
+    _QiboBackend = object
+
+# GATE_OPS, cpu.py:23-36
+GATE_OPS = {
+    "X": "apply_x",
+    "CNOT": "apply_x",
+    "TOFFOLI": "apply_x",
+    "Y": "apply_y",
+    "Z": "apply_z",
+    "CY": "apply_y",
+    "CZ": "apply_z",
+    "U1": "apply_z_pow",
+    "CU1": "apply_z_pow",
+    "SWAP": "apply_swap",
+    "fSim": "apply_fsim",
+    "GeneralizedfSim": "apply_fsim",
+}
+
+# qibo's SHOT_METROPOLIS_THRESHOLD: below it qibo samples directly
+SHOT_METROPOLIS_THRESHOLD = 100000
+
+_TORCH_DTYPES = None
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _torch_dtype(name: str):
+    global _TORCH_DTYPES
+    if _TORCH_DTYPES is None:
+        t = _torch()
+        _TORCH_DTYPES = {"complex128": t.complex128, "complex64": t.complex64,
+                         "float64": t.float64, "float32": t.float32, "int64": t.int64,
+                         "int32": t.int32}
+    return _TORCH_DTYPES[name]
+
+
+def _dtype_name(x) -> str:
+    s = str(x)
+    return s.replace("torch.", "").replace("numpy.", "").replace("<class '", "").replace("'>", "")
+
+
+class GB300Backend(_QiboBackend):
+    """State-vector backend running on one GB300 through the engine's C ABI."""
+
+    def __init__(self, device: int = 0):
+        if _QiboBackend is not object:
+            super().__init__()
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise ImportError("Could not detect a CUDA device for the gb300 platform.")
+        self.name = "qibojit"
+        self.platform = "gb300"
+        self.device_index = int(device)
+        self.device = f"/GPU:{device}"
+        self._tdevice = torch.device("cuda", self.device_index)
+        torch.cuda.set_device(self._tdevice)
+        self.ctx = _lib.Context(self.device_index)
+        self.lib = self.ctx.lib
+        self.dtype = "complex128"
+        self.matrices = Matrices(self.dtype)
+        self.custom_matrices = CustomMatrices(self.dtype)
+        try:
+            self.nthreads = len(os.sched_getaffinity(0))
+        except AttributeError:  # pragma: no cover
+            self.nthreads = os.cpu_count() or 1
+        self.versions = {"qibojit_gb300": "0.1.0", "engine": self.lib.sv_version()}
+        self.tensor_types = (np.ndarray, torch.Tensor)
+        self.supports_multigpu = False
+
+    # ------------------------------------------------------------------ setters
+    def set_dtype(self, dtype) -> None:
+        dtype = _dtype_name(dtype)
+        if dtype not in _lib.DTYPE_CODES:
+            raise ValueError(f"Unsupported dtype {dtype}.")
+        self.dtype = dtype
+        self.matrices = Matrices(dtype)
+        self.custom_matrices = CustomMatrices(dtype)
+
+    def set_device(self, device: str) -> None:
+        if "GPU" not in device:
+            raise ValueError(f"Device {device} is not available for {self} backend.")
+        idx = int(device.split(":")[-1]) if ":" in device else 0
+        if idx != self.device_index:
+            raise ValueError(f"Device {device} is not available for {self} backend (bound to GPU:{self.device_index}).")
+
+    def set_threads(self, nthreads: int) -> None:
+        """Number of Metropolis chains (the reference uses one chain per CPU thread)."""
+        self.nthreads = int(nthreads)
+
+    def set_seed(self, seed) -> None:
+        if seed is not None:
+            np.random.seed(seed)
+
+    def __repr__(self):
+        return "qibojit (gb300)"
+
+    # ------------------------------------------------------------ array plumbing
+    def cast(self, array, dtype=None, copy: bool = False):
+        torch = _torch()
+        dtype = _dtype_name(dtype) if dtype is not None else self.dtype
+        tdt = _torch_dtype(dtype)
+        if isinstance(array, torch.Tensor):
+            out = array.to(device=self._tdevice, dtype=tdt)
+            if copy and out.data_ptr() == array.data_ptr():
+                out = out.clone()
+            return out.contiguous()
+        arr = np.asarray(array, dtype=dtype)
+        return torch.from_numpy(np.ascontiguousarray(arr)).to(self._tdevice)
+
+    def to_numpy(self, array):
+        torch = _torch()
+        if isinstance(array, torch.Tensor):
+            return array.detach().cpu().numpy()
+        return np.asarray(array)
+
+    def _check_state(self, state, nqubits: Optional[int] = None) -> int:
+        torch = _torch()
+        if not isinstance(state, torch.Tensor) or not state.is_cuda:
+            raise TypeError("GB300Backend operates on CUDA tensors; use backend.cast(state) first.")
+        if not state.is_contiguous():
+            raise ValueError("state must be contiguous")
+        if nqubits is not None and state.numel() != (1 << int(nqubits)):
+            raise ValueError(f"state has {state.numel()} amplitudes, not 2^{nqubits}")
+        name = _dtype_name(state.dtype)
+        if name not in _lib.DTYPE_CODES:
+            raise TypeError(f"unsupported state dtype {name}")
+        return _lib.DTYPE_CODES[name]
+
+    def _operand(self, matrix, dtype: str):
+        torch = _torch()
+        if isinstance(matrix, torch.Tensor):
+            matrix = matrix.detach().cpu().numpy()
+        return np.ascontiguousarray(np.asarray(matrix, dtype=dtype).ravel())
+
+    # -------------------------------------------------------------- state creation
+    def zero_state(self, nqubits: int, density_matrix: bool = False, dtype=None):
+        if density_matrix:
+            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+        dtype = _dtype_name(dtype) if dtype is not None else self.dtype
+        torch = _torch()
+        state = torch.empty(1 << nqubits, dtype=_torch_dtype(dtype), device=self._tdevice)
+        _lib.check(self.lib.sv_zero_state(self.ctx.handle, state.data_ptr(), _lib.DTYPE_CODES[dtype], int(nqubits)),
+                   "zero_state")
+        return state
+
+    # ------------------------------------------------------------- gate dispatch
+    def apply_gate(self, gate, state, nqubits: int, inverse: bool = False):
+        if len(tuple(state.shape)) == 2:
+            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+        return self._apply_gate(gate, state, nqubits)
+
+    def _create_qubits_tensor(self, gate, nqubits: int):
+        qubits = [nqubits - q - 1 for q in gate.control_qubits]
+        qubits.extend(nqubits - q - 1 for q in gate.target_qubits)
+        return np.array(sorted(qubits), dtype=np.int32)
+
+    def _as_custom_matrix(self, gate, dtype: Optional[str] = None):
+        """Kernel operand of a gate (cpu.py:519-539)."""
+        dtype = dtype or self.dtype
+        cm = self.custom_matrices if dtype == self.dtype else CustomMatrices(dtype)
+        name = type(gate).__name__
+        if name == "FusedGate":
+            from .fusion import matrix_fused
+
+            return matrix_fused(gate, dtype)
+        if name == "Unitary":
+            return self._operand(gate.parameters[0], dtype)
+        _matrix = getattr(cm, name)
+        if name == "FanOut":
+            return cm.X
+        if getattr(gate, "parameters", ()) and callable(_matrix):
+            if name == "GeneralizedRBS":  # pragma: no cover
+                raise NotImplementedError("GeneralizedRBS is not supported")
+            return _matrix(*gate.parameters)
+        return _matrix(2 ** len(gate.target_qubits)) if callable(_matrix) else _matrix
+
+    def _apply_gate(self, gate, state, nqubits: int):
+        dtype = _dtype_name(state.dtype)
+        if getattr(gate, "name", "") == "fanout":
+            return self._apply_fanout_gate(gate, state, nqubits)
+        matrix = self._as_custom_matrix(gate, dtype)
+        qubits = self._create_qubits_tensor(gate, nqubits)
+        targets = gate.target_qubits
+        if len(targets) == 1:
+            op = GATE_OPS.get(type(gate).__name__, "apply_gate")
+            return self._one_qubit_base(state, nqubits, *targets, op, matrix, qubits)
+        if len(targets) == 2:
+            op = GATE_OPS.get(type(gate).__name__, "apply_two_qubit_gate")
+            return self._two_qubit_base(state, nqubits, *targets, op, matrix, qubits)
+        return self._multi_qubit_base(state, nqubits, targets, matrix, qubits)
+
+    def _apply_fanout_gate(self, gate, state, nqubits: int):
+        control = gate.control_qubits[0]
+        x = self.custom_matrices.X
+        for target in gate.target_qubits:
+            qubits = np.array(sorted([nqubits - control - 1, nqubits - target - 1]), dtype=np.int32)
+            state = self._one_qubit_base(state, nqubits, target, "apply_x", x, qubits)
+        return state
+
+    def _one_qubit_base(self, state, nqubits: int, target: int, kernel: str, gate, qubits):
+        dt = self._check_state(state, nqubits)
+        op = self._operand(gate, _dtype_name(state.dtype)) if kernel in ("apply_gate", "apply_z_pow") else None
+        q, nq = _lib.int32_array(qubits if qubits is not None else [])
+        rc = self.lib.sv_apply_one_qubit(self.ctx.handle, state.data_ptr(), dt, int(nqubits),
+                                         _lib.ONE_KINDS[kernel], None if op is None else op.ctypes.data,
+                                         int(target), q, nq)
+        _lib.check(rc, kernel)
+        return state
+
+    def _two_qubit_base(self, state, nqubits: int, target1: int, target2: int, kernel: str, gate, qubits):
+        dt = self._check_state(state, nqubits)
+        op = self._operand(gate, _dtype_name(state.dtype)) if kernel != "apply_swap" else None
+        q, nq = _lib.int32_array(qubits if qubits is not None else [])
+        rc = self.lib.sv_apply_two_qubit(self.ctx.handle, state.data_ptr(), dt, int(nqubits),
+                                         _lib.TWO_KINDS[kernel], None if op is None else op.ctypes.data,
+                                         int(target1), int(target2), q, nq)
+        _lib.check(rc, kernel)
+        return state
+
+    def _multi_qubit_base(self, state, nqubits: int, targets, gate, qubits):
+        dt = self._check_state(state, nqubits)
+        op = self._operand(gate, _dtype_name(state.dtype))
+        t, nt = _lib.int32_array(list(targets))
+        if op.size != 1 << (2 * nt):
+            raise ValueError(f"a gate on {nt} targets needs a {1 << nt}x{1 << nt} matrix")
+        q, nq = _lib.int32_array(qubits if qubits is not None else [])
+        rc = self.lib.sv_apply_multi_qubit(self.ctx.handle, state.data_ptr(), dt, int(nqubits), op.ctypes.data,
+                                           t, nt, q, nq)
+        _lib.check(rc, "apply_multi_qubit_gate")
+        return state
+
+    # ------------------------------------------------------------------ collapse
+    def collapse_state(self, state, qubits: Sequence[int], shot, nqubits: int, normalize: bool = True,
+                       density_matrix: bool = False):
+        if density_matrix:
+            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+        dt = self._check_state(state, nqubits)
+        if hasattr(shot, "shape"):
+            shot = int(np.asarray(self.to_numpy(shot)).ravel()[0])
+        elif hasattr(shot, "__len__"):
+            shot = int(shot[0])
+        q, nq = _lib.int32_array(list(qubits))
+        rc = self.lib.sv_collapse_state(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, int(shot),
+                                        int(bool(normalize)))
+        _lib.check(rc, "collapse_state")
+        return state
+
+    # -------------------------------------------------------------- probabilities
+    def calculate_probabilities(self, state, qubits: Sequence[int], nqubits: int, density_matrix: bool = False,
+                                out_dtype: Optional[str] = None):
+        """|psi|^2 marginalised on ``qubits``; float64 for complex128 states and float32
+        for complex64 states (the state's real type, as qibo returns), summed in FP64."""
+        if density_matrix:
+            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+        dt = self._check_state(state, nqubits)
+        if out_dtype is None:
+            out_dtype = "float64" if dt in (_lib.SV_C128, _lib.SV_F64) else "float32"
+        torch = _torch()
+        out = torch.empty(1 << len(qubits), dtype=_torch_dtype(out_dtype), device=self._tdevice)
+        q, nq = _lib.int32_array(list(qubits))
+        rc = self.lib.sv_probabilities(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, out.data_ptr(),
+                                       _lib.DTYPE_CODES[out_dtype])
+        _lib.check(rc, "calculate_probabilities")
+        return out
+
+    # ------------------------------------------------------------------ sampling
+    def measure_frequencies_op(self, frequencies, probs, nshots: int, nqubits: int, seed: int, nthreads: int):
+        """ops.measure_frequencies (ops.py:82-108) on the GPU: same chains, same streams,
+        same frequencies.  ``frequencies`` and ``probs`` may be numpy arrays (copied in and
+        out) or CUDA tensors (updated in place)."""
+        torch = _torch()
+        host_out = None
+        if not isinstance(frequencies, torch.Tensor):
+            host_out = frequencies
+            frequencies = torch.zeros(len(frequencies), dtype=torch.int64, device=self._tdevice)
+            work = frequencies
+        elif frequencies.dtype != torch.int64:
+            work = torch.zeros(frequencies.shape[0], dtype=torch.int64, device=self._tdevice)
+        else:
+            work = frequencies
+        probs = self.cast(probs, dtype=_dtype_name(probs.dtype))
+        pdt = _lib.DTYPE_CODES[_dtype_name(probs.dtype)]
+        if pdt not in (_lib.SV_F64, _lib.SV_F32):
+            raise TypeError("probabilities must be float32 or float64")
+        nstates = int(probs.shape[0])
+        nbits = nstates.bit_length() - 1
+        if nstates != 1 << nbits or work.shape[0] != nstates:
+            raise ValueError("frequencies and probabilities need 2^n entries")
+        rc = self.lib.sv_measure_frequencies(self.ctx.handle, work.data_ptr(), probs.data_ptr(), pdt, nbits,
+                                             int(nshots), int(seed) & 0xFFFFFFFF, int(nthreads))
+        _lib.check(rc, "measure_frequencies")
+        if host_out is not None:
+            host_out += work.cpu().numpy().astype(host_out.dtype)
+            return host_out
+        if work is not frequencies:
+            frequencies += work.to(frequencies.dtype)
+        return frequencies
+
+    def sample_frequencies(self, probabilities, nshots: int) -> Counter:
+        seed = int(np.random.randint(0, int(1e8)))
+        probs = self.cast(probabilities, dtype=_dtype_name(getattr(probabilities, "dtype", "float64")))
+        if _dtype_name(probs.dtype) not in ("float64", "float32"):
+            probs = probs.real.contiguous()
+        torch = _torch()
+        freqs = torch.zeros(probs.shape[0], dtype=torch.int64, device=self._tdevice)
+        freqs = self.measure_frequencies_op(freqs, probs, nshots, 0, seed, self.nthreads)
+        idx = torch.nonzero(freqs).flatten()
+        return Counter(dict(zip(idx.cpu().tolist(), freqs[idx].cpu().tolist())))
+
+    # ---------------------------------------------------------------- execution
+    def execute_circuit(self, circuit, initial_state=None, nshots: Optional[int] = None):
+        """Applies ``circuit.queue`` gate by gate (qibo's plain method) and returns the state."""
+        n = circuit.nqubits
+        if initial_state is None:
+            state = self.zero_state(n)
+        else:
+            state = self.cast(initial_state, dtype=_dtype_name(getattr(initial_state, "dtype", self.dtype)),
+                              copy=True)
+        for gate in circuit.queue:
+            state = self.apply_gate(gate, state, n)
+        return state
+
+    def assert_allclose(self, value, target, rtol=1e-7, atol=0.0):
+        np.testing.assert_allclose(self.to_numpy(value), self.to_numpy(target), rtol=rtol, atol=atol)
+
+    def synchronize(self) -> None:
+        self.ctx.sync()

@@ -1,0 +1,470 @@
+// sv_gates.cu -- per-gate state-vector kernels (the "plain method") and their C ABI.
+//
+// One kernel launch is one read-modify-write pass over the amplitudes a gate touches.
+// Thread t of block b handles ITEMS index groups b*256*ITEMS + t + j*256: all loads of
+// a thread are issued before any arithmetic, so every thread keeps ITEMS independent
+// 16/8-byte requests in flight, and consecutive threads touch consecutive amplitudes
+// for every target position (two coalesced streams 2^m apart for a target at bit m).
+//
+// Index maps follow the reference kernels (qibojit src/qibojit/custom_operators/
+// gates.py): an uncontrolled gate inserts a 0 at the target bit(s); a controlled gate
+// inserts a 1 at every sorted control/target bit (multicontrol_index, gates.py:5-12)
+// and steps back from that all-ones index.  Arithmetic uses fused multiply-adds, so
+// results match the reference to rounding (<= a few ulp per gate), not bit for bit.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sv_common.cuh"
+
+namespace sv {
+
+constexpr int kBlock = 256;
+
+template <typename T, int N>
+struct Mat {
+  T g[N];
+};
+
+// ------------------------------------------------------------------ one target
+template <typename T, int KIND, bool CTRL, int ITEMS>
+__global__ void __launch_bounds__(kBlock) k_one_qubit(T* __restrict__ s, int64_t nstates, int m,
+                                                      Mat<T, 4> g, const __grid_constant__ BitList q) {
+  const int64_t tk = (int64_t)1 << m;
+  const int64_t base = (int64_t)blockIdx.x * (kBlock * ITEMS) + threadIdx.x;
+  int64_t i1[ITEMS];
+  T a[ITEMS], b[ITEMS];
+  constexpr bool kReadsLow = (KIND == SV_APPLY_GATE || KIND == SV_APPLY_X || KIND == SV_APPLY_Y);
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    const int64_t gi = base + (int64_t)j * kBlock;
+    i1[j] = -1;
+    if (gi < nstates) {
+      if (CTRL) i1[j] = insert_ones(gi, q) - tk;
+      else i1[j] = insert_zero(gi, m);
+      if (kReadsLow) a[j] = ldg_stream(s + i1[j]);
+      b[j] = ldg_stream(s + i1[j] + tk);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    if (i1[j] < 0) continue;
+    T* p = s + i1[j];
+    if constexpr (KIND == SV_APPLY_GATE) {
+      T x, y;
+      if constexpr (is_complex<T>::value) {
+        x = cmad2(g.g[0], a[j], g.g[1], b[j]);
+        y = cmad2(g.g[2], a[j], g.g[3], b[j]);
+      } else {
+        x = fma(g.g[0], a[j], g.g[1] * b[j]);
+        y = fma(g.g[2], a[j], g.g[3] * b[j]);
+      }
+      stg_stream(p, x);
+      stg_stream(p + tk, y);
+    } else if constexpr (KIND == SV_APPLY_X) {
+      stg_stream(p, b[j]);
+      stg_stream(p + tk, a[j]);
+    } else if constexpr (KIND == SV_APPLY_Y) {
+      if constexpr (is_complex<T>::value) {
+        // (a, b) <- (-i b, i a)
+        T x, y;
+        x.re = b[j].im; x.im = -b[j].re;
+        y.re = -a[j].im; y.im = a[j].re;
+        stg_stream(p, x);
+        stg_stream(p + tk, y);
+      }
+    } else if constexpr (KIND == SV_APPLY_Z) {
+      stg_stream(p + tk, tneg(b[j]));
+    } else {  // SV_APPLY_Z_POW
+      stg_stream(p + tk, tmul(g.g[0], b[j]));
+    }
+  }
+}
+
+// ------------------------------------------------------------------ two targets
+template <typename T, int KIND, bool CTRL, int ITEMS>
+__global__ void __launch_bounds__(kBlock) k_two_qubit(T* __restrict__ s, int64_t nstates, int m1,
+                                                      int m2, int swap_targets, Mat<T, 16> g,
+                                                      const __grid_constant__ BitList q) {
+  const int64_t tk1 = (int64_t)1 << m1, tk2 = (int64_t)1 << m2;
+  const int64_t uk1 = swap_targets ? tk2 : tk1;
+  const int64_t uk2 = swap_targets ? tk1 : tk2;
+  const int64_t base = (int64_t)blockIdx.x * (kBlock * ITEMS) + threadIdx.x;
+  int64_t i0[ITEMS];
+  T v[ITEMS][4];
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    const int64_t gi = base + (int64_t)j * kBlock;
+    i0[j] = -1;
+    if (gi < nstates) {
+      if (CTRL) i0[j] = insert_ones(gi, q) - tk1 - tk2;
+      else i0[j] = insert_zero(insert_zero(gi, m1), m2);
+      if constexpr (KIND == SV_APPLY_TWO_QUBIT_GATE) {
+        v[j][0] = ldg_stream(s + i0[j]);
+        v[j][3] = ldg_stream(s + i0[j] + tk1 + tk2);
+      }
+      if constexpr (KIND == SV_APPLY_FSIM) v[j][3] = ldg_stream(s + i0[j] + tk1 + tk2);
+      v[j][1] = ldg_stream(s + i0[j] + uk1);
+      v[j][2] = ldg_stream(s + i0[j] + uk2);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    if (i0[j] < 0) continue;
+    T* p = s + i0[j];
+    if constexpr (KIND == SV_APPLY_TWO_QUBIT_GATE) {
+      T o[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        T acc = tmul(g.g[4 * r + 3], v[j][3]);
+        acc = tfma(g.g[4 * r + 2], v[j][2], acc);
+        acc = tfma(g.g[4 * r + 1], v[j][1], acc);
+        o[r] = tfma(g.g[4 * r + 0], v[j][0], acc);
+      }
+      stg_stream(p, o[0]);
+      stg_stream(p + uk1, o[1]);
+      stg_stream(p + uk2, o[2]);
+      stg_stream(p + tk1 + tk2, o[3]);
+    } else if constexpr (KIND == SV_APPLY_SWAP) {
+      stg_stream(p + uk1, v[j][2]);
+      stg_stream(p + uk2, v[j][1]);
+    } else {  // fSim: 2x2 on (|01>, |10>) and a phase on |11>
+      const T x = tfma(g.g[0], v[j][1], tmul(g.g[1], v[j][2]));
+      const T y = tfma(g.g[2], v[j][1], tmul(g.g[3], v[j][2]));
+      stg_stream(p + uk1, x);
+      stg_stream(p + uk2, y);
+      stg_stream(p + tk1 + tk2, tmul(g.g[4], v[j][3]));
+    }
+  }
+}
+
+// ------------------------------------------------------------ k targets, registers
+// One thread per group of 2^K amplitudes; the 4^K matrix rides in the kernel
+// parameters (4 KB for K = 4, complex128).  Local row index bit u <-> stride ts[u].
+struct Strides {
+  int64_t ts[kMaxTargets];
+  int64_t zero_off;  // sum of the target strides: all-ones index -> group origin
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kBlock) k_multi_reg(T* __restrict__ s, int64_t ngroups,
+                                                      Mat<T, (1 << (2 * K))> g, const __grid_constant__ BitList q,
+                                                      const __grid_constant__ Strides st) {
+  constexpr int N = 1 << K;
+  const int64_t gi = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (gi >= ngroups) return;
+  const int64_t i0 = insert_ones(gi, q) - st.zero_off;
+  int64_t off[N];
+  T in[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    int64_t o = 0;
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if ((i >> u) & 1) o += st.ts[u];
+    off[i] = o;
+    in[i] = ldg_stream(s + i0 + o);
+  }
+#pragma unroll
+  for (int r = 0; r < N; r++) {
+    T acc = tmul(g.g[r * N], in[0]);
+#pragma unroll
+    for (int c = 1; c < N; c++) acc = tfma(g.g[r * N + c], in[c], acc);
+    stg_stream(s + i0 + off[r], acc);
+  }
+}
+
+// ------------------------------------------------- k targets, shared-memory groups
+// A block stages NG groups (NG * 2^k amplitudes, <= 32 KB) in shared memory, laid
+// out [row][group] so that consecutive threads read consecutive groups, then every
+// thread forms some outputs as dot products with a matrix row read from global
+// memory (L1-resident, warp-uniform).  Outputs go straight back to HBM.
+constexpr int kSmemBytes = 32 * 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_multi_smem(T* __restrict__ s, int64_t ngroups, int k,
+                                                       const T* __restrict__ gmat, const __grid_constant__ BitList q,
+                                                       const __grid_constant__ Strides st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* buf = reinterpret_cast<T*>(smem_raw);
+  const int N = 1 << k;
+  const int NG = (int)(kSmemBytes / sizeof(T)) / N;  // groups per block (>= 1)
+  const int64_t g0 = (int64_t)blockIdx.x * NG;
+  const int total = NG * N;
+  for (int e = threadIdx.x; e < total; e += kBlock) {
+    const int i = e / NG, gg = e - i * NG;
+    const int64_t gi = g0 + gg;
+    if (gi < ngroups) {
+      int64_t o = 0;
+      for (int u = 0; u < k; u++)
+        if ((i >> u) & 1) o += st.ts[u];
+      buf[e] = ldg_stream(s + insert_ones(gi, q) - st.zero_off + o);
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < total; e += kBlock) {
+    const int r = e / NG, gg = e - r * NG;
+    const int64_t gi = g0 + gg;
+    if (gi >= ngroups) continue;
+    const T* row = gmat + (size_t)r * N;
+    T acc = tzero<T>();
+    for (int c = 0; c < N; c++) acc = tfma(ldg_ro(row + c), buf[c * NG + gg], acc);
+    int64_t o = 0;
+    for (int u = 0; u < k; u++)
+      if ((r >> u) & 1) o += st.ts[u];
+    stg_stream(s + insert_ones(gi, q) - st.zero_off + o, acc);
+  }
+}
+
+// =============================================================== host side
+static int check_state_args(const void* state, int dtype, int nqubits) {
+  if (!state) return set_error(SV_ERR_ARG, "state pointer is NULL");
+  if (dtype < SV_C128 || dtype > SV_F32) return set_error(SV_ERR_ARG, "unknown dtype %d", dtype);
+  if (nqubits < 1 || nqubits > kMaxQubits)
+    return set_error(SV_ERR_ARG, "nqubits = %d out of range [1, %d]", nqubits, kMaxQubits);
+  if (((uintptr_t)state) % dtype_size(dtype))
+    return set_error(SV_ERR_ARG, "state pointer is not aligned to its element size");
+  return SV_OK;
+}
+
+// Builds the sorted bit list of a gate.  `qubits` (if given) must be sorted, unique,
+// in range, and contain every target bit; otherwise the target bits alone are used.
+static int make_bitlist(BitList* out, int nqubits, const int* target_bits, int ntargets,
+                        const int32_t* qubits, int nq) {
+  std::vector<int> bits;
+  if (qubits && nq > 0) {
+    bits.assign(qubits, qubits + nq);
+  } else {
+    bits.assign(target_bits, target_bits + ntargets);
+    std::sort(bits.begin(), bits.end());
+  }
+  if ((int)bits.size() > nqubits || (int)bits.size() > kMaxQubits)
+    return set_error(SV_ERR_ARG, "gate acts on %d qubits of a %d-qubit state", (int)bits.size(), nqubits);
+  for (size_t j = 0; j < bits.size(); j++) {
+    if (bits[j] < 0 || bits[j] >= nqubits)
+      return set_error(SV_ERR_ARG, "qubit bit position %d out of range for %d qubits", bits[j], nqubits);
+    if (j > 0 && bits[j] <= bits[j - 1])
+      return set_error(SV_ERR_ARG, "qubits tensor must be sorted and free of duplicates");
+  }
+  for (int t = 0; t < ntargets; t++)
+    if (!std::binary_search(bits.begin(), bits.end(), target_bits[t]))
+      return set_error(SV_ERR_ARG, "target bit %d missing from the qubits tensor", target_bits[t]);
+  out->n = (int)bits.size();
+  for (size_t j = 0; j < bits.size(); j++) out->pos[j] = bits[j];
+  return SV_OK;
+}
+
+template <typename T, int KIND, bool CTRL>
+static int launch_one(Context* ctx, void* state, int64_t nstates, int m, const Mat<T, 4>& g,
+                      const BitList& q) {
+  constexpr int ITEMS = 4;
+  const unsigned grid = grid_for(nstates, kBlock * ITEMS);
+  k_one_qubit<T, KIND, CTRL, ITEMS><<<grid, kBlock, 0, ctx->stream>>>((T*)state, nstates, m, g, q);
+  SV_LAUNCH_CHECK("one-qubit kernel launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int one_qubit_typed(Context* ctx, void* state, int nqubits, int kind, const void* gate,
+                           int target, const BitList& q, bool ctrl) {
+  Mat<T, 4> g;
+  memset(&g, 0, sizeof(g));
+  if (kind == SV_APPLY_GATE) {
+    if (!gate) return set_error(SV_ERR_ARG, "apply_gate needs a 2x2 operand");
+    memcpy(g.g, gate, 4 * sizeof(T));
+  } else if (kind == SV_APPLY_Z_POW) {
+    if (!gate) return set_error(SV_ERR_ARG, "apply_z_pow needs its phase operand");
+    memcpy(g.g, gate, sizeof(T));
+  }
+  const int m = nqubits - target - 1;
+  const int ncontrols = q.n - 1;
+  const int64_t nstates = (int64_t)1 << (nqubits - ncontrols - 1);
+#define SV_ONE_CASE(KIND)                                                   \
+  case KIND:                                                                \
+    return ctrl ? launch_one<T, KIND, true>(ctx, state, nstates, m, g, q)   \
+                : launch_one<T, KIND, false>(ctx, state, nstates, m, g, q);
+  switch (kind) {
+    SV_ONE_CASE(SV_APPLY_GATE)
+    SV_ONE_CASE(SV_APPLY_X)
+    SV_ONE_CASE(SV_APPLY_Z)
+    SV_ONE_CASE(SV_APPLY_Z_POW)
+    case SV_APPLY_Y:
+      if constexpr (is_complex<T>::value) {
+        return ctrl ? launch_one<T, SV_APPLY_Y, true>(ctx, state, nstates, m, g, q)
+                    : launch_one<T, SV_APPLY_Y, false>(ctx, state, nstates, m, g, q);
+      } else {
+        return set_error(SV_ERR_UNSUPPORTED, "apply_y needs a complex state");
+      }
+    default:
+      return set_error(SV_ERR_ARG, "unknown one-qubit kernel %d", kind);
+  }
+#undef SV_ONE_CASE
+}
+
+template <typename T, int KIND, bool CTRL>
+static int launch_two(Context* ctx, void* state, int64_t nstates, int m1, int m2, int swap,
+                      const Mat<T, 16>& g, const BitList& q) {
+  constexpr int ITEMS = 2;
+  const unsigned grid = grid_for(nstates, kBlock * ITEMS);
+  k_two_qubit<T, KIND, CTRL, ITEMS><<<grid, kBlock, 0, ctx->stream>>>((T*)state, nstates, m1, m2,
+                                                                      swap, g, q);
+  SV_LAUNCH_CHECK("two-qubit kernel launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int two_qubit_typed(Context* ctx, void* state, int nqubits, int kind, const void* gate,
+                           int target1, int target2, const BitList& q, bool ctrl) {
+  Mat<T, 16> g;
+  memset(&g, 0, sizeof(g));
+  if (kind == SV_APPLY_TWO_QUBIT_GATE) {
+    if (!gate) return set_error(SV_ERR_ARG, "apply_two_qubit_gate needs a 4x4 operand");
+    memcpy(g.g, gate, 16 * sizeof(T));
+  } else if (kind == SV_APPLY_FSIM) {
+    if (!gate) return set_error(SV_ERR_ARG, "apply_fsim needs its 5-entry operand");
+    memcpy(g.g, gate, 5 * sizeof(T));
+  }
+  // cpu.py:618-635: m1 < m2 always; swap the row order when target1 > target2
+  int m1, m2, swap;
+  if (target1 > target2) {
+    swap = 1;
+    m1 = nqubits - target1 - 1;
+    m2 = nqubits - target2 - 1;
+  } else {
+    swap = 0;
+    m1 = nqubits - target2 - 1;
+    m2 = nqubits - target1 - 1;
+  }
+  const int ncontrols = q.n - 2;
+  const int64_t nstates = (int64_t)1 << (nqubits - 2 - ncontrols);
+#define SV_TWO_CASE(KIND)                                                             \
+  case KIND:                                                                          \
+    return ctrl ? launch_two<T, KIND, true>(ctx, state, nstates, m1, m2, swap, g, q)  \
+                : launch_two<T, KIND, false>(ctx, state, nstates, m1, m2, swap, g, q);
+  switch (kind) {
+    SV_TWO_CASE(SV_APPLY_TWO_QUBIT_GATE)
+    SV_TWO_CASE(SV_APPLY_SWAP)
+    SV_TWO_CASE(SV_APPLY_FSIM)
+    default:
+      return set_error(SV_ERR_ARG, "unknown two-qubit kernel %d", kind);
+  }
+#undef SV_TWO_CASE
+}
+
+template <typename T, int K>
+static int launch_multi_reg(Context* ctx, void* state, int64_t ngroups, const void* gate,
+                            const BitList& q, const Strides& st) {
+  Mat<T, (1 << (2 * K))> g;
+  memcpy(g.g, gate, sizeof(g.g));
+  k_multi_reg<T, K><<<grid_for(ngroups, kBlock), kBlock, 0, ctx->stream>>>((T*)state, ngroups, g, q, st);
+  SV_LAUNCH_CHECK("multi-qubit kernel launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int multi_qubit_typed(Context* ctx, void* state, int nqubits, const void* gate,
+                             const int32_t* targets, int k, const BitList& q) {
+  Strides st;
+  memset(&st, 0, sizeof(st));
+  for (int u = 0; u < k; u++) {
+    st.ts[u] = (int64_t)1 << (nqubits - targets[k - 1 - u] - 1);
+    st.zero_off += st.ts[u];
+  }
+  const int64_t ngroups = (int64_t)1 << (nqubits - q.n);
+  switch (k) {
+    case 1: return launch_multi_reg<T, 1>(ctx, state, ngroups, gate, q, st);
+    case 2: return launch_multi_reg<T, 2>(ctx, state, ngroups, gate, q, st);
+    case 3: return launch_multi_reg<T, 3>(ctx, state, ngroups, gate, q, st);
+    case 4:
+      if (sizeof(T) <= 8) return launch_multi_reg<T, 4>(ctx, state, ngroups, gate, q, st);
+      break;
+    default: break;
+  }
+  const size_t mbytes = sizeof(T) << (2 * k);
+  SV_TRY(ensure_operand(ctx, mbytes));
+  SV_TRY(check_cuda(cudaMemcpyAsync(ctx->operand, gate, mbytes, cudaMemcpyHostToDevice, ctx->stream),
+                    "gate operand upload"));
+  const int NG = (int)(kSmemBytes / sizeof(T)) >> k;
+  if (NG < 1) return set_error(SV_ERR_ARG, "%d targets exceed the shared-memory group size", k);
+  const int64_t nblocks = (ngroups + NG - 1) / NG;
+  k_multi_smem<T><<<(unsigned)nblocks, kBlock, kSmemBytes, ctx->stream>>>(
+      (T*)state, ngroups, k, (const T*)ctx->operand, q, st);
+  SV_LAUNCH_CHECK("multi-qubit (shared) kernel launch");
+  return SV_OK;
+}
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" {
+
+int sv_apply_one_qubit(sv_context* ctx, void* state, int dtype, int nqubits, int kind,
+                       const void* gate, int target, const int32_t* qubits, int nq) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state_args(state, dtype, nqubits));
+  if (target < 0 || target >= nqubits)
+    return set_error(SV_ERR_ARG, "target %d out of range for %d qubits", target, nqubits);
+  const int tbit = nqubits - target - 1;
+  BitList q;
+  SV_TRY(make_bitlist(&q, nqubits, &tbit, 1, qubits, nq));
+  const bool ctrl = q.n > 1;
+  Context* c = ctx;
+  switch (dtype) {
+    case SV_C128: return one_qubit_typed<c128>(c, state, nqubits, kind, gate, target, q, ctrl);
+    case SV_C64: return one_qubit_typed<c64>(c, state, nqubits, kind, gate, target, q, ctrl);
+    case SV_F64: return one_qubit_typed<double>(c, state, nqubits, kind, gate, target, q, ctrl);
+    default: return one_qubit_typed<float>(c, state, nqubits, kind, gate, target, q, ctrl);
+  }
+}
+
+int sv_apply_two_qubit(sv_context* ctx, void* state, int dtype, int nqubits, int kind,
+                       const void* gate, int target1, int target2, const int32_t* qubits, int nq) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state_args(state, dtype, nqubits));
+  if (target1 < 0 || target1 >= nqubits || target2 < 0 || target2 >= nqubits || target1 == target2)
+    return set_error(SV_ERR_ARG, "targets (%d, %d) invalid for %d qubits", target1, target2, nqubits);
+  if (kind == SV_APPLY_FSIM && (dtype == SV_F64 || dtype == SV_F32))
+    return set_error(SV_ERR_UNSUPPORTED, "apply_fsim needs a complex state");
+  const int tb[2] = {nqubits - target1 - 1, nqubits - target2 - 1};
+  BitList q;
+  SV_TRY(make_bitlist(&q, nqubits, tb, 2, qubits, nq));
+  const bool ctrl = q.n > 2;
+  Context* c = ctx;
+  switch (dtype) {
+    case SV_C128: return two_qubit_typed<c128>(c, state, nqubits, kind, gate, target1, target2, q, ctrl);
+    case SV_C64: return two_qubit_typed<c64>(c, state, nqubits, kind, gate, target1, target2, q, ctrl);
+    case SV_F64: return two_qubit_typed<double>(c, state, nqubits, kind, gate, target1, target2, q, ctrl);
+    default: return two_qubit_typed<float>(c, state, nqubits, kind, gate, target1, target2, q, ctrl);
+  }
+}
+
+int sv_apply_multi_qubit(sv_context* ctx, void* state, int dtype, int nqubits, const void* gate,
+                         const int32_t* targets, int ntargets, const int32_t* qubits, int nq) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state_args(state, dtype, nqubits));
+  if (!gate || !targets) return set_error(SV_ERR_ARG, "gate and targets are required");
+  if (ntargets < 1 || ntargets > kMaxTargets || ntargets > nqubits)
+    return set_error(SV_ERR_ARG, "Number of target qubits must be <= %d but is %d.", kMaxTargets, ntargets);
+  int tb[kMaxTargets];
+  for (int t = 0; t < ntargets; t++) {
+    if (targets[t] < 0 || targets[t] >= nqubits)
+      return set_error(SV_ERR_ARG, "target %d out of range for %d qubits", targets[t], nqubits);
+    for (int u = 0; u < t; u++)
+      if (targets[u] == targets[t]) return set_error(SV_ERR_ARG, "duplicate target %d", targets[t]);
+    tb[t] = nqubits - targets[t] - 1;
+  }
+  BitList q;
+  SV_TRY(make_bitlist(&q, nqubits, tb, ntargets, qubits, nq));
+  Context* c = ctx;
+  switch (dtype) {
+    case SV_C128: return multi_qubit_typed<c128>(c, state, nqubits, gate, targets, ntargets, q);
+    case SV_C64: return multi_qubit_typed<c64>(c, state, nqubits, gate, targets, ntargets, q);
+    case SV_F64: return multi_qubit_typed<double>(c, state, nqubits, gate, targets, ntargets, q);
+    default: return multi_qubit_typed<float>(c, state, nqubits, gate, targets, ntargets, q);
+  }
+}
+
+}  // extern "C"

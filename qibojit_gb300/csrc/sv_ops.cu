@@ -1,0 +1,625 @@
+// sv_ops.cu -- state creation, collapse, probabilities and Metropolis sampling.
+//
+// Everything stays on the device and on the context's stream: the collapse norm is
+// reduced, square-rooted and inverted by kernels (no host round trip), and the
+// sampler runs NumPy's legacy MT19937 streams on the GPU, one warp per chain.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sv_common.cuh"
+
+namespace sv {
+
+constexpr int kOpsBlock = 256;
+
+// ----------------------------------------------------------------- zero state
+// |0...0>, ops.py:10-18: 16-byte stores of zeros, the first chunk holding 1.0.
+__global__ void k_fill_zero_state(uint4* __restrict__ p, int64_t nchunks, uint4 first) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += stride)
+    __stcs(p + c, c == 0 ? first : make_uint4(0, 0, 0, 0));
+}
+__global__ void k_set_first(unsigned char* p, int bytes, uint4 first) {
+  const unsigned char* f = reinterpret_cast<const unsigned char*>(&first);
+  for (int b = threadIdx.x; b < bytes; b += blockDim.x) p[b] = b < 16 ? f[b] : 0;
+}
+
+// ------------------------------------------------------------ block reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Neumaier-compensated accumulation of one term.
+struct KSum {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return s + c; }
+};
+
+// Block-wide sum of `v` in a fixed order; the result is valid in thread 0.
+__device__ double block_sum(double v) {
+  __shared__ double part[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) part[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------------ collapse
+// Measured bits: `mask` has a 1 at every measured bit position, `value` holds the
+// outcome bits at those positions.  An amplitude is kept iff (i & mask) == value.
+// kept_index(g) enumerates the kept amplitudes in increasing order by inserting the
+// outcome bits at the sorted measured positions (ops.py:33-40, collapse_index).
+struct Measured {
+  int n;
+  int pos[kMaxQubits];   // sorted ascending bit positions
+  int bit[kMaxQubits];   // outcome bit at pos[j]
+  int64_t mask, value;
+};
+
+__device__ __forceinline__ int64_t kept_index(int64_t g, const Measured& m) {
+  int64_t i = g;
+  for (int j = 0; j < m.n; j++) {
+    const int p = m.pos[j];
+    const int64_t k = (int64_t)1 << p;
+    i = ((i >> p) << (p + 1)) + (i & (k - 1)) + (m.bit[j] ? k : 0);
+  }
+  return i;
+}
+
+// Pass 1 (normalize only): per-block compensated partial sums of |kept|^2.
+template <typename T>
+__global__ void __launch_bounds__(kOpsBlock) k_collapse_norm_partials(
+    const T* __restrict__ s, int64_t nkept, const __grid_constant__ Measured m,
+    double* __restrict__ partials) {
+  KSum acc;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nkept; g += stride)
+    acc.add(tnorm2(ldg_stream(s + kept_index(g, m))));
+  const double r = block_sum(acc.value());
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+}
+
+// Sums the partials in a fixed order (compensated) and stores 1/sqrt(sum).
+__global__ void k_finish_inverse_norm(const double* __restrict__ partials, int np,
+                                      double* __restrict__ out) {
+  KSum acc;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) acc.add(partials[i]);
+  __shared__ double sh_s[kOpsBlock], sh_c[kOpsBlock];
+  sh_s[threadIdx.x] = acc.s;
+  sh_c[threadIdx.x] = acc.c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    KSum t;
+    for (int i = 0; i < (int)blockDim.x; i++) {
+      t.add(sh_s[i]);
+      t.add(sh_c[i]);
+    }
+    const double norm2 = t.value();
+    out[0] = norm2;
+    out[1] = 1.0 / sqrt(norm2);  // NumPy divides a complex by a real as a product with 1/x
+  }
+}
+
+// Pass 2: zero the amplitudes of other outcomes (write-only) and, when normalizing,
+// scale the kept ones by the inverse norm computed on the device.
+template <typename T, bool NORMALIZE>
+__global__ void __launch_bounds__(kOpsBlock) k_collapse_apply(T* __restrict__ s, int64_t n,
+                                                             int64_t mask, int64_t value,
+                                                             const double* __restrict__ inv) {
+  using R = typename real_of<T>::type;
+  const R scale = NORMALIZE ? (R)inv[1] : (R)1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    if ((i & mask) != value) {
+      stg_stream(s + i, tzero<T>());
+    } else if (NORMALIZE) {
+      T a = ldg_stream(s + i);
+      if constexpr (is_complex<T>::value) {
+        a.re *= scale;
+        a.im *= scale;
+      } else {
+        a *= scale;
+      }
+      stg_stream(s + i, a);
+    }
+  }
+}
+
+// ------------------------------------------------------------- probabilities
+struct ProbMap {
+  int n, nq;
+  int mpos[kMaxQubits];     // bit position feeding output bit (nq-1-j), j = 0..nq-1
+  int sorted[kMaxQubits];   // measured bit positions, ascending (for inserting zeros)
+};
+
+// amplitude index of (output bin o, unmeasured index u)
+__device__ __forceinline__ int64_t prob_index(int64_t o, int64_t u, const ProbMap& p) {
+  int64_t i = u;
+  for (int j = 0; j < p.nq; j++) {
+    const int b = p.sorted[j];
+    const int64_t k = (int64_t)1 << b;
+    i = ((i >> b) << (b + 1)) + (i & (k - 1));
+  }
+  for (int j = 0; j < p.nq; j++)
+    if ((o >> (p.nq - 1 - j)) & 1) i |= (int64_t)1 << p.mpos[j];
+  return i;
+}
+
+template <typename T, typename O>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_full(const T* __restrict__ s, int64_t n,
+                                                          O* __restrict__ out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    __stcs(out + i, (O)tnorm2(ldg_stream(s + i)));
+}
+
+// all qubits measured in a permuted order: out[perm(i)] = |a_i|^2
+template <typename T, typename O>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_perm(const T* __restrict__ s, int64_t n,
+                                                          const __grid_constant__ ProbMap p,
+                                                          O* __restrict__ out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    int64_t o = 0;
+    for (int j = 0; j < p.nq; j++) o |= ((i >> p.mpos[j]) & 1) << (p.nq - 1 - j);
+    out[o] = (O)tnorm2(ldg_stream(s + i));
+  }
+}
+
+// few amplitudes per bin: one thread per bin, sequential sum
+template <typename T, typename O>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_thread_bins(const T* __restrict__ s,
+                                                                 int64_t nbins, int64_t per_bin,
+                                                                 const __grid_constant__ ProbMap p,
+                                                                 O* __restrict__ out) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nbins) return;
+  double acc = 0.0;
+  for (int64_t u = 0; u < per_bin; u++) acc += tnorm2(ldg_stream(s + prob_index(o, u, p)));
+  out[o] = (O)acc;
+}
+
+// many amplitudes per bin: block (segment, bin) sums a contiguous range of u
+template <typename T>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restrict__ s,
+                                                              int64_t per_bin, int nseg,
+                                                              const __grid_constant__ ProbMap p,
+                                                              double* __restrict__ partials) {
+  const int64_t o = blockIdx.y;
+  const int seg = blockIdx.x;
+  const int64_t len = per_bin / nseg;
+  const int64_t u0 = (int64_t)seg * len;
+  double acc = 0.0;
+  for (int64_t u = u0 + threadIdx.x; u < u0 + len; u += blockDim.x)
+    acc += tnorm2(ldg_stream(s + prob_index(o, u, p)));
+  const double r = block_sum(acc);
+  if (threadIdx.x == 0) partials[o * nseg + seg] = r;
+}
+
+template <typename O>
+__global__ void k_probs_finish(const double* __restrict__ partials, int64_t nbins, int nseg,
+                               O* __restrict__ out) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nbins) return;
+  double acc = 0.0;
+  for (int k = 0; k < nseg; k++) acc += partials[o * nseg + k];
+  out[o] = (O)acc;
+}
+
+// ------------------------------------------------------------ Metropolis sampler
+// NumPy legacy MT19937 (Matsumoto & Nishimura 1998): init_genrand seeding, the
+// twist over 624 words, and tempering on output.
+constexpr int kMT = 624;
+
+__host__ __device__ inline uint32_t mt_temper(uint32_t y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+__host__ __device__ inline uint32_t mt_twist(uint32_t cur, uint32_t next, uint32_t src) {
+  const uint32_t y = (cur & 0x80000000u) | (next & 0x7fffffffu);
+  return src ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+
+struct HostMT {
+  uint32_t mt[kMT];
+  int pos;
+  explicit HostMT(uint32_t seed) {
+    mt[0] = seed;
+    for (int i = 1; i < kMT; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+    pos = kMT;
+  }
+  uint32_t next() {
+    if (pos >= kMT) {
+      for (int k = 0; k < kMT; k++) mt[k] = mt_twist(mt[k], mt[(k + 1) % kMT], mt[(k + 397) % kMT]);
+      pos = 0;
+    }
+    return mt_temper(mt[pos++]);
+  }
+  // NumPy legacy randint(0, high): masked rejection on one 32-bit word
+  uint32_t randint(uint64_t high) {
+    const uint64_t rng = high - 1;
+    if (rng == 0) return 0;
+    uint64_t mask = rng;
+    mask |= mask >> 1; mask |= mask >> 2; mask |= mask >> 4; mask |= mask >> 8; mask |= mask >> 16;
+    uint64_t v;
+    do { v = next() & mask; } while (v > rng);
+    return (uint32_t)v;
+  }
+};
+
+// One warp regenerates the 624-word block in place, 32 words at a time, in the
+// sequential algorithm's order (words below 227 read the old word k+397, later words
+// the new word k-227; each chunk reads before it writes).
+__device__ void mt_regenerate_warp(uint32_t* mt, int lane) {
+  for (int base = 0; base < kMT; base += 32) {
+    const int k = base + lane;
+    uint32_t nv = 0;
+    if (k < kMT) {
+      const uint32_t cur = mt[k];
+      const uint32_t nxt = mt[(k + 1) % kMT];
+      const uint32_t src = k < 227 ? mt[k + 397] : mt[k - 227];
+      nv = mt_twist(cur, nxt, src);
+    }
+    __syncwarp();
+    // (the last word pairs with word 0, already renewed by the first chunk)
+    if (k < kMT) mt[k] = nv;
+    __syncwarp();
+  }
+}
+
+struct Chain {
+  uint32_t seed;
+  int64_t nshots;
+};
+
+constexpr int kChainWarps = 4;  // chains per block
+
+// Every lane of the warp follows the chain (warp-uniform control flow); lane 0 keeps
+// the histogram.  Each step draws randint(0, N) (one word, N = 2^nbits so the mask
+// never rejects) and random() (two words), exactly as ops.py:100-106 consumes them.
+template <typename P>
+__global__ void __launch_bounds__(32 * kChainWarps) k_metropolis(
+    const P* __restrict__ probs, uint32_t mask, const Chain* __restrict__ chains, int nchains,
+    const int64_t* __restrict__ start, unsigned long long* __restrict__ freq) {
+  __shared__ uint32_t mt_all[kChainWarps][kMT];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kChainWarps + w;
+  if (c >= nchains) return;
+  uint32_t* mt = mt_all[w];
+  if (lane == 0) {
+    mt[0] = chains[c].seed;
+    for (int i = 1; i < kMT; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+  }
+  __syncwarp();
+  int pos = kMT;
+  const int64_t nshots = chains[c].nshots;
+  uint64_t shot = (uint64_t)start[0];
+  P pshot = probs[shot];
+  auto next_word = [&]() -> uint32_t {
+    if (pos >= kMT) {
+      mt_regenerate_warp(mt, lane);
+      pos = 0;
+    }
+    return mt_temper(mt[pos++]);
+  };
+  for (int64_t i = 0; i < nshots; i++) {
+    const uint32_t w0 = next_word();
+    const uint32_t w1 = next_word();
+    const uint32_t w2 = next_word();
+    const uint64_t nshot = (shot + (uint64_t)(w0 & mask)) & (uint64_t)mask;
+    const double r = ((double)(w1 >> 5) * 67108864.0 + (double)(w2 >> 6)) / 9007199254740992.0;
+    const P pnew = probs[nshot];
+    bool accept;
+    if constexpr (sizeof(P) == 8) accept = (pnew / pshot) > r;
+    else accept = (pnew / pshot) > __double2float_rn(r);
+    if (accept) {
+      shot = nshot;
+      pshot = pnew;
+    }
+    if (lane == 0) atomicAdd(freq + shot, 1ull);
+  }
+}
+
+// Chain seeds: np.random.seed(seed); [randint(0, 1e8) for each chain], ops.py:92-93.
+// Shots: nshots // nchains each, the remainder on the last chain (ops.py:88-90).
+static void make_chains(uint32_t seed, int64_t nshots, int nchains, std::vector<Chain>* out) {
+  HostMT m(seed);
+  out->resize(nchains);
+  for (int c = 0; c < nchains; c++) {
+    (*out)[c].seed = m.randint(100000000u);
+    (*out)[c].nshots = nshots / nchains;
+  }
+  (*out)[nchains - 1].nshots += nshots % nchains;
+}
+
+// first index of the maximum: per-block (value, index) then one final block
+template <typename P>
+__global__ void k_argmax_partials(const P* __restrict__ p, int64_t n, P* __restrict__ bv,
+                                  int64_t* __restrict__ bi) {
+  P best = p[0];
+  int64_t idx = 0;
+  bool have = false;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const P v = p[i];
+    if (!have || v > best) {  // strided in increasing order: keeps the first maximum
+      best = v;
+      idx = i;
+      have = true;
+    }
+  }
+  __shared__ P sv[kOpsBlock];
+  __shared__ int64_t si[kOpsBlock];
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = have ? idx : INT64_MAX;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    P b = sv[0];
+    int64_t bidx = si[0];
+    for (int t = 1; t < (int)blockDim.x; t++) {
+      if (si[t] == INT64_MAX) continue;
+      if (bidx == INT64_MAX || sv[t] > b || (sv[t] == b && si[t] < bidx)) {
+        b = sv[t];
+        bidx = si[t];
+      }
+    }
+    bv[blockIdx.x] = b;
+    bi[blockIdx.x] = bidx;
+  }
+}
+
+template <typename P>
+__global__ void k_argmax_finish(const P* __restrict__ bv, const int64_t* __restrict__ bi, int nb,
+                                int64_t* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  P b = bv[0];
+  int64_t idx = bi[0];
+  for (int k = 1; k < nb; k++) {
+    if (bi[k] == INT64_MAX) continue;
+    if (idx == INT64_MAX || bv[k] > b || (bv[k] == b && bi[k] < idx)) {
+      b = bv[k];
+      idx = bi[k];
+    }
+  }
+  out[0] = idx == INT64_MAX ? 0 : idx;
+}
+
+// =================================================================== host side
+static int check_state(const void* state, int dtype, int nqubits) {
+  if (!state) return set_error(SV_ERR_ARG, "state pointer is NULL");
+  if (dtype < SV_C128 || dtype > SV_F32) return set_error(SV_ERR_ARG, "unknown dtype %d", dtype);
+  if (nqubits < 1 || nqubits > kMaxQubits)
+    return set_error(SV_ERR_ARG, "nqubits = %d out of range [1, %d]", nqubits, kMaxQubits);
+  if (((uintptr_t)state) % dtype_size(dtype))
+    return set_error(SV_ERR_ARG, "state pointer is not aligned to its element size");
+  return SV_OK;
+}
+
+static unsigned stream_grid(const Context* ctx, int64_t work) {
+  const int64_t cap = (int64_t)ctx->num_sms * 8;
+  int64_t g = (work + kOpsBlock - 1) / kOpsBlock;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+static int zero_state_impl(Context* ctx, void* state, int dtype, int nqubits) {
+  SV_TRY(check_state(state, dtype, nqubits));
+  const size_t bytes = dtype_size(dtype) << nqubits;
+  uint4 first = make_uint4(0, 0, 0, 0);
+  if (dtype == SV_C128 || dtype == SV_F64) {
+    const double one = 1.0;
+    memcpy(&first, &one, sizeof(one));
+  } else {
+    const float one = 1.0f;
+    memcpy(&first, &one, sizeof(one));
+  }
+  if (bytes >= 16 && ((uintptr_t)state % 16) == 0 && bytes % 16 == 0) {
+    const int64_t nchunks = (int64_t)(bytes / 16);
+    k_fill_zero_state<<<stream_grid(ctx, nchunks), kOpsBlock, 0, ctx->stream>>>((uint4*)state, nchunks, first);
+  } else {
+    k_set_first<<<1, 32, 0, ctx->stream>>>((unsigned char*)state, (int)bytes, first);
+  }
+  SV_LAUNCH_CHECK("zero_state launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int collapse_typed(Context* ctx, void* state, int nqubits, const Measured& m, int normalize) {
+  const int64_t n = (int64_t)1 << nqubits;
+  double* inv = nullptr;
+  if (normalize) {
+    const int64_t nkept = (int64_t)1 << (nqubits - m.n);
+    const unsigned grid = stream_grid(ctx, nkept);
+    SV_TRY(ensure_scratch(ctx, (grid + 2) * sizeof(double)));
+    double* partials = (double*)ctx->scratch;
+    inv = partials + grid;
+    k_collapse_norm_partials<T><<<grid, kOpsBlock, 0, ctx->stream>>>((const T*)state, nkept, m, partials);
+    SV_LAUNCH_CHECK("collapse norm launch");
+    k_finish_inverse_norm<<<1, kOpsBlock, 0, ctx->stream>>>(partials, (int)grid, inv);
+    SV_LAUNCH_CHECK("collapse norm finish launch");
+    k_collapse_apply<T, true><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>((T*)state, n, m.mask, m.value, inv);
+  } else {
+    k_collapse_apply<T, false><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>((T*)state, n, m.mask, m.value, nullptr);
+  }
+  SV_LAUNCH_CHECK("collapse launch");
+  return SV_OK;
+}
+
+template <typename T, typename O>
+static int probs_typed(Context* ctx, const void* state, int nqubits, const ProbMap& p, void* out) {
+  const int64_t n = (int64_t)1 << nqubits;
+  const T* s = (const T*)state;
+  if (p.nq == nqubits) {
+    bool identity = true;
+    for (int j = 0; j < p.nq; j++) identity &= (p.mpos[j] == nqubits - 1 - j);
+    if (identity) k_probs_full<T, O><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, (O*)out);
+    else k_probs_perm<T, O><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, p, (O*)out);
+    SV_LAUNCH_CHECK("probabilities launch");
+    return SV_OK;
+  }
+  const int64_t nbins = (int64_t)1 << p.nq;
+  const int64_t per_bin = (int64_t)1 << (nqubits - p.nq);
+  if (per_bin <= 64 || nbins > 65535 || nbins >= (int64_t)ctx->num_sms * 4 * kOpsBlock) {
+    k_probs_thread_bins<T, O><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(s, nbins, per_bin, p, (O*)out);
+    SV_LAUNCH_CHECK("probabilities launch");
+    return SV_OK;
+  }
+  // segments per bin: enough blocks to fill the GPU, each summing >= 4096 amplitudes
+  int64_t nseg = ((int64_t)ctx->num_sms * 8 + nbins - 1) / nbins;
+  while (nseg > 1 && per_bin / nseg < 4096) nseg >>= 1;
+  int64_t pow2 = 1;
+  while (pow2 * 2 <= nseg) pow2 *= 2;
+  nseg = pow2;  // per_bin is a power of two: segments divide it exactly
+  SV_TRY(ensure_scratch(ctx, (size_t)(nbins * nseg) * sizeof(double)));
+  double* partials = (double*)ctx->scratch;
+  dim3 grid((unsigned)nseg, (unsigned)nbins);
+  k_probs_segments<T><<<grid, kOpsBlock, 0, ctx->stream>>>(s, per_bin, (int)nseg, p, partials);
+  SV_LAUNCH_CHECK("probabilities launch");
+  k_probs_finish<O><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(partials, nbins, (int)nseg, (O*)out);
+  SV_LAUNCH_CHECK("probabilities finish launch");
+  return SV_OK;
+}
+
+template <typename P>
+static int sample_typed(Context* ctx, int64_t* freq, const void* probs, int nbits, int64_t nshots,
+                        uint32_t seed, int nchains) {
+  const int64_t n = (int64_t)1 << nbits;
+  std::vector<Chain> chains;
+  make_chains(seed, nshots, nchains, &chains);
+  const unsigned gblocks = stream_grid(ctx, n);
+  // scratch layout: [chains][argmax block values][argmax block indices][start]
+  const size_t chain_bytes = ((sizeof(Chain) * nchains + 255) / 256) * 256;
+  const size_t val_bytes = ((sizeof(P) * gblocks + 255) / 256) * 256;
+  const size_t idx_bytes = ((sizeof(int64_t) * gblocks + 255) / 256) * 256;
+  SV_TRY(ensure_scratch(ctx, chain_bytes + val_bytes + idx_bytes + 256));
+  unsigned char* base = (unsigned char*)ctx->scratch;
+  Chain* d_chains = (Chain*)base;
+  P* d_bv = (P*)(base + chain_bytes);
+  int64_t* d_bi = (int64_t*)(base + chain_bytes + val_bytes);
+  int64_t* d_start = (int64_t*)(base + chain_bytes + val_bytes + idx_bytes);
+  // the chain table is small; a synchronous copy keeps the host vector's lifetime simple
+  SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "sampler (sync)"));
+  SV_TRY(check_cuda(cudaMemcpy(d_chains, chains.data(), sizeof(Chain) * nchains, cudaMemcpyHostToDevice),
+                    "sampler chain upload"));
+  k_argmax_partials<P><<<gblocks, kOpsBlock, 0, ctx->stream>>>((const P*)probs, n, d_bv, d_bi);
+  SV_LAUNCH_CHECK("argmax launch");
+  k_argmax_finish<P><<<1, 32, 0, ctx->stream>>>(d_bv, d_bi, (int)gblocks, d_start);
+  SV_LAUNCH_CHECK("argmax finish launch");
+  const uint32_t mask = (uint32_t)(n - 1);
+  k_metropolis<P><<<grid_for(nchains, kChainWarps), 32 * kChainWarps, 0, ctx->stream>>>(
+      (const P*)probs, mask, d_chains, nchains, d_start, (unsigned long long*)freq);
+  SV_LAUNCH_CHECK("metropolis launch");
+  return SV_OK;
+}
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" {
+
+int sv_zero_state(sv_context* ctx, void* state, int dtype, int nqubits) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  return zero_state_impl(ctx, state, dtype, nqubits);
+}
+
+int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits, const int32_t* qubits,
+                      int nq, int64_t result, int normalize) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state(state, dtype, nqubits));
+  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "collapse needs 1..n measured qubits");
+  if (result < 0 || result >= ((int64_t)1 << nq))
+    return set_error(SV_ERR_ARG, "outcome %lld out of range for %d qubits", (long long)result, nq);
+  Measured m;
+  memset(&m, 0, sizeof(m));
+  m.n = nq;
+  std::vector<std::pair<int, int>> pb;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits)
+      return set_error(SV_ERR_ARG, "measured qubit %d out of range", qubits[j]);
+    const int pos = nqubits - qubits[j] - 1;
+    const int bit = (int)((result >> (nq - 1 - j)) & 1);
+    for (auto& e : pb)
+      if (e.first == pos) return set_error(SV_ERR_ARG, "duplicate measured qubit %d", qubits[j]);
+    pb.push_back({pos, bit});
+    m.mask |= (int64_t)1 << pos;
+    if (bit) m.value |= (int64_t)1 << pos;
+  }
+  std::sort(pb.begin(), pb.end());
+  for (int j = 0; j < nq; j++) {
+    m.pos[j] = pb[j].first;
+    m.bit[j] = pb[j].second;
+  }
+  switch (dtype) {
+    case SV_C128: return collapse_typed<c128>(ctx, state, nqubits, m, normalize);
+    case SV_C64: return collapse_typed<c64>(ctx, state, nqubits, m, normalize);
+    case SV_F64: return collapse_typed<double>(ctx, state, nqubits, m, normalize);
+    default: return collapse_typed<float>(ctx, state, nqubits, m, normalize);
+  }
+}
+
+int sv_probabilities(sv_context* ctx, const void* state, int dtype, int nqubits, const int32_t* qubits,
+                     int nq, void* out, int out_dtype) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state(state, dtype, nqubits));
+  if (!out) return set_error(SV_ERR_ARG, "output pointer is NULL");
+  if (out_dtype != SV_F64 && out_dtype != SV_F32) return set_error(SV_ERR_ARG, "out_dtype must be SV_F64 or SV_F32");
+  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "probabilities need 1..n qubits");
+  ProbMap p;
+  memset(&p, 0, sizeof(p));
+  p.n = nqubits;
+  p.nq = nq;
+  std::vector<int> sorted;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits) return set_error(SV_ERR_ARG, "qubit %d out of range", qubits[j]);
+    p.mpos[j] = nqubits - qubits[j] - 1;
+    sorted.push_back(p.mpos[j]);
+  }
+  std::sort(sorted.begin(), sorted.end());
+  for (int j = 0; j < nq; j++) {
+    if (j > 0 && sorted[j] == sorted[j - 1]) return set_error(SV_ERR_ARG, "duplicate qubit in probabilities");
+    p.sorted[j] = sorted[j];
+  }
+  const bool f64 = out_dtype == SV_F64;
+  switch (dtype) {
+    case SV_C128: return f64 ? probs_typed<c128, double>(ctx, state, nqubits, p, out) : probs_typed<c128, float>(ctx, state, nqubits, p, out);
+    case SV_C64: return f64 ? probs_typed<c64, double>(ctx, state, nqubits, p, out) : probs_typed<c64, float>(ctx, state, nqubits, p, out);
+    case SV_F64: return f64 ? probs_typed<double, double>(ctx, state, nqubits, p, out) : probs_typed<double, float>(ctx, state, nqubits, p, out);
+    default: return f64 ? probs_typed<float, double>(ctx, state, nqubits, p, out) : probs_typed<float, float>(ctx, state, nqubits, p, out);
+  }
+}
+
+int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* probs, int prob_dtype,
+                           int nbits, int64_t nshots, uint32_t seed, int nchains) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  if (!frequencies || !probs) return set_error(SV_ERR_ARG, "frequencies and probs are required");
+  if (nbits < 0 || nbits > 32) return set_error(SV_ERR_ARG, "nbits = %d out of range [0, 32]", nbits);
+  if (nchains < 1 || nchains > (1 << 20)) return set_error(SV_ERR_ARG, "nchains = %d out of range", nchains);
+  if (nshots < 0) return set_error(SV_ERR_ARG, "nshots must be >= 0");
+  if (prob_dtype == SV_F64) return sample_typed<double>(ctx, frequencies, probs, nbits, nshots, seed, nchains);
+  if (prob_dtype == SV_F32) return sample_typed<float>(ctx, frequencies, probs, nbits, nshots, seed, nchains);
+  return set_error(SV_ERR_ARG, "prob_dtype must be SV_F64 or SV_F32");
+}
+
+}  // extern "C"
