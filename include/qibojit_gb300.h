@@ -114,6 +114,26 @@ int sv_apply_multi_qubit(sv_context* ctx, void* state, int dtype, int nqubits,
 int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits,
                       const int32_t* qubits, int nq, int64_t result, int normalize);
 
+/* Same collapse as sv_collapse_state, for callers that cannot allocate device
+ * memory: code running inside a host framework that owns every device byte through
+ * its own pool allocator, or a latency-critical loop that cannot afford a cudaMalloc
+ * or the device synchronisation of a later cudaFree.  It takes no context and calls
+ * no cudaMalloc, cudaFree or allocating library routine; the caller passes the
+ * state (device pointer) and the measured qubits/outcome (host), and the work is
+ * enqueued on `stream` (a cudaStream_t as void*, NULL = legacy default stream) on
+ * the current device.  The norm reduction uses a fixed file-scope device array of
+ * 4096 doubles (32 KiB), held by every GPU that loads the library until the process
+ * exits; a call whose reduction would need more (more than 4094 partial sums, i.e.
+ * a GPU with more than 511 SMs) is rejected with SV_ERR_ARG.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) with the
+ * device current, so make that first call before any stream capture.  All calls
+ * share the array and it keeps the last call's contents (every call overwrites what
+ * it reads, nothing needs to start at zero); calls that overlap on the GPU (different
+ * streams, or different host threads on one device) race on it.
+ * This entry point has no counterpart in the reference. */
+int sv_collapse_state_noalloc(void* stream, void* state, int dtype, int nqubits,
+                              const int32_t* qubits, int nq, int64_t result, int normalize);
+
 /* ----------------------------------------------------------- probabilities */
 /* out[o] = sum of |amp|^2 over amplitudes whose measured bits spell o, with
  * qubits[0] the most significant bit of o (qibo Backend.calculate_probabilities,

@@ -27,6 +27,7 @@ EXPORTS = (
     "sv_version", "sv_last_error", "sv_device_count", "sv_context_create", "sv_context_destroy",
     "sv_context_set_stream", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
     "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_measure_frequencies",
+    "sv_collapse_state_noalloc",
 )
 
 
@@ -57,6 +58,7 @@ _SIGNATURES = {
     "sv_collapse_state": ([_vp, _vp, _int, _int, _vp, _int, _i64, _int], _int),
     "sv_probabilities": ([_vp, _vp, _int, _int, _vp, _int, _vp, _int], _int),
     "sv_measure_frequencies": ([_vp, _vp, _vp, _int, _int, _i64, ctypes.c_uint32, _int], _int),
+    "sv_collapse_state_noalloc": ([_vp, _vp, _int, _int, _vp, _int, _i64, _int], _int),
 }
 
 

@@ -623,3 +623,123 @@ int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* pr
 }
 
 }  // extern "C"
+
+// ============================================== collapse without device allocation
+// Callers that cannot call cudaMalloc (a host framework that owns every device byte
+// through its own pool allocator, or a latency-critical loop where an allocation and
+// the device synchronisation of a later cudaFree are not acceptable) use
+// sv_collapse_state_noalloc.  Its reduction scratch is the file-scope array below,
+// which every GPU that loads this library holds until the process exits.
+#include <mutex>
+
+namespace sv {
+
+constexpr int kNoAllocScratchDoubles = 4096;  // 32 KiB: norm partials + (norm^2, 1/norm)
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_collapse_scratch[kNoAllocScratchDoubles];
+
+struct NoAllocDevice {
+  bool ready = false;
+  double* scratch = nullptr;  // device address of g_noalloc_collapse_scratch on this device
+  int num_sms = 0;
+};
+static NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+// Once per device, with that device current: the array's name is only a host-side
+// stand-in, so its device address must come from cudaGetSymbolAddress.
+static int noalloc_setup(int device, NoAllocDevice** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocDevice& d = g_noalloc_devices[device];
+  if (!d.ready) {
+    void* ptr = nullptr;
+    SV_TRY(check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_collapse_scratch),
+                      "cudaGetSymbolAddress(no-alloc collapse scratch)"));
+    int sms = 0;
+    SV_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device),
+                      "cudaDeviceGetAttribute"));
+    d.scratch = static_cast<double*>(ptr);
+    d.num_sms = sms;
+    d.ready = true;
+  }
+  *out = &d;
+  return SV_OK;
+}
+
+template <typename T>
+static int collapse_noalloc_typed(cudaStream_t stream, const NoAllocDevice& d, void* state, int nqubits,
+                                  const Measured& m, int normalize) {
+  const int64_t n = (int64_t)1 << nqubits;
+  const int64_t cap = (int64_t)d.num_sms * 8;
+  auto grid_of = [cap](int64_t work) {
+    int64_t g = (work + kOpsBlock - 1) / kOpsBlock;
+    return (unsigned)(g > cap ? cap : (g < 1 ? 1 : g));
+  };
+  if (!normalize) {
+    k_collapse_apply<T, false><<<grid_of(n), kOpsBlock, 0, stream>>>((T*)state, n, m.mask, m.value, nullptr);
+    SV_LAUNCH_CHECK("no-alloc collapse launch");
+    return SV_OK;
+  }
+  const int64_t nkept = (int64_t)1 << (nqubits - m.n);
+  const unsigned grid = grid_of(nkept);
+  // every block writes its own partial and the finish kernel writes both results
+  // before the apply pass reads them, so nothing left from an earlier call is read
+  if ((int64_t)grid + 2 > kNoAllocScratchDoubles)
+    return set_error(SV_ERR_ARG,
+                     "no-alloc collapse needs %u doubles of scratch; its static array holds at most %d",
+                     grid + 2, kNoAllocScratchDoubles);
+  double* partials = d.scratch;
+  double* inv = d.scratch + grid;
+  k_collapse_norm_partials<T><<<grid, kOpsBlock, 0, stream>>>((const T*)state, nkept, m, partials);
+  SV_LAUNCH_CHECK("no-alloc collapse norm launch");
+  k_finish_inverse_norm<<<1, kOpsBlock, 0, stream>>>(partials, (int)grid, inv);
+  SV_LAUNCH_CHECK("no-alloc collapse norm finish launch");
+  k_collapse_apply<T, true><<<grid_of(n), kOpsBlock, 0, stream>>>((T*)state, n, m.mask, m.value, inv);
+  SV_LAUNCH_CHECK("no-alloc collapse launch");
+  return SV_OK;
+}
+
+}  // namespace sv
+
+extern "C" int sv_collapse_state_noalloc(void* stream, void* state, int dtype, int nqubits,
+                                         const int32_t* qubits, int nq, int64_t result, int normalize) {
+  using namespace sv;
+  SV_TRY(check_state(state, dtype, nqubits));
+  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "collapse needs 1..n measured qubits");
+  if (result < 0 || result >= ((int64_t)1 << nq))
+    return set_error(SV_ERR_ARG, "outcome %lld out of range for %d qubits", (long long)result, nq);
+  Measured m;
+  memset(&m, 0, sizeof(m));
+  m.n = nq;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits)
+      return set_error(SV_ERR_ARG, "measured qubit %d out of range", qubits[j]);
+    const int pos = nqubits - qubits[j] - 1;
+    if (m.mask & ((int64_t)1 << pos)) return set_error(SV_ERR_ARG, "duplicate measured qubit %d", qubits[j]);
+    m.mask |= (int64_t)1 << pos;
+    if ((result >> (nq - 1 - j)) & 1) m.value |= (int64_t)1 << pos;
+  }
+  // measured positions in ascending order, each with its outcome bit
+  int k = 0;
+  for (int p = 0; p < nqubits; p++) {
+    if (!(m.mask & ((int64_t)1 << p))) continue;
+    m.pos[k] = p;
+    m.bit[k] = (int)((m.value >> p) & 1);
+    k++;
+  }
+  int device = 0;
+  SV_TRY(check_cuda(cudaGetDevice(&device), "cudaGetDevice"));
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return set_error(SV_ERR_ARG, "device %d beyond the %d devices the no-alloc path tracks", device,
+                     kNoAllocMaxDevices);
+  NoAllocDevice* d = nullptr;
+  SV_TRY(noalloc_setup(device, &d));
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (dtype) {
+    case SV_C128: return collapse_noalloc_typed<c128>(s, *d, state, nqubits, m, normalize);
+    case SV_C64: return collapse_noalloc_typed<c64>(s, *d, state, nqubits, m, normalize);
+    case SV_F64: return collapse_noalloc_typed<double>(s, *d, state, nqubits, m, normalize);
+    default: return collapse_noalloc_typed<float>(s, *d, state, nqubits, m, normalize);
+  }
+}
