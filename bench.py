@@ -1,16 +1,25 @@
-"""Benchmark: seeded random brickwork circuit on n=30 qubits, depth 20, complex128.
+"""Benchmark: seeded random brickwork circuit on n=30 qubits, depth 20.
 
-One step = |0...0> followed by the 890 gates of the circuit (600 U3 + 290 CZ),
-applied by the GB300 engine on a 16 GiB state resident in HBM (larger than the
-129 MB L2, so no flush is needed between steps).  The metric is gate-applications
-per second for the whole job; ``roofline`` reports the dominant kernel (the dense
-one-target U3 pass) against the measured HBM copy bandwidth; ``e2e`` repeats the
-metric through the public backend API with the initial state uploaded from pinned
-host memory and the final state read back every step; ``cpu_baseline`` times the
-CPU restatement of the reference kernels on a bounded sample (the first layer).
+Workload: every layer applies U3(t, p, l) (angles i.i.d. uniform [0, 2pi) from the
+seed) to all 30 qubits, then CZ on disjoint nearest-neighbour pairs alternating even
+and odd offsets: 600 U3 + 290 CZ = 890 gates, starting from |0...0>.
 
-``--impl reference`` times the reference's CPU algorithm (the oracle's C/OpenMP
-restatement of the Numba kernels, all host threads) on the same workload.
+One step = |0...0> followed by the 890 gates, run by the GB300 engine's fused
+(cache-blocked) path in complex64 — the precision mode whose bulk gate arithmetic is
+complex64 and whose reductions are FP64 — on a state resident in HBM (8 GiB, larger
+than the 129 MB L2, so no flush is needed between steps).  ``value`` is whole-job
+gate-applications/s.  The same run also times, once each, the complex128 fused path,
+the complex64 and complex128 per-gate (plain) paths, and reports the complex64
+result's infidelity and max amplitude error against the complex128 state.
+
+``roofline`` covers the dominant kernel (the fused pass): achieved = algorithmic bytes
+of one pass (2 x 8 B x 2^30, one read and one write of the state) / its mean duration
+from CUDA events over the timed region; FP32 arithmetic is reported beside it
+(16 flops per amplitude per dense one-qubit gate).  ``e2e`` repeats the metric
+through the public backend API (``execute_circuit``) with the initial state uploaded
+from pinned host memory and the final state read back every step.
+``cpu_baseline`` and ``--impl reference`` time the CPU restatement of the reference's
+Numba kernels (per-gate, OpenMP, all host threads) on the first layer of the circuit.
 """
 from __future__ import annotations
 
@@ -28,28 +37,32 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "gate-applications/s (brickwork n=30 depth 20)"
-UNIT = "gates/s"
 N_QUBITS = 30
 DEPTH = 20
 SEED = 1234
 FALLBACK_HBM_GBS = 6800.0
+FP32_PEAK_TFLOPS = 73.3  # FP32 FMA rate measured on this GPU type by a probe (2 flops per FMA)
+
+
+def metric_name(n: int) -> str:
+    return f"gate-applications/s (brickwork n={n} depth {DEPTH})"
+
+
+UNIT = "gates/s"
 
 
 def _peak_hbm():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def _traffic_from_profiles(kernel_key: str):
-    """dram bytes per launch recorded in the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", f"{kernel_key}.md")
+def _traffic_from_profiles(key: str):
+    """DRAM bytes per launch recorded in the committed ncu summary, or None."""
     try:
-        for line in open(path):
+        for line in open(os.path.join(ROOT, "profiles", f"{key}.md")):
             if line.startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":", 1)[1].strip())
     except OSError:
@@ -108,32 +121,25 @@ class ClockSampler:
                     reasons.add(nm)
         if not sms:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sms)}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    return ws, rank
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
 
 
-def cpu_baseline_oracle(n: int, sample_layers: int = 1, threads: int = None):
-    """Times the oracle's per-gate restatement of the reference kernels on the first
-    `sample_layers` layers of the brickwork circuit at full size."""
+def cpu_baseline_oracle(n: int, dtype: str, sample_layers: int = 1):
+    """The oracle's per-gate restatement of the reference kernels, first layer(s) of the circuit."""
     from oracle import pyoracle as O
     from qibojit_gb300 import circuits
     from qibojit_gb300.matrices import CustomMatrices
 
-    if threads:
-        O.set_threads(threads)
     cores = O.max_threads()
     circ = circuits.brickwork(n, DEPTH, SEED)
-    per_layer = n + (n // 2)
-    gates = circ.queue[: per_layer * sample_layers]
-    cm = CustomMatrices("complex128")
+    gates = circ.queue[: (n + n // 2) * sample_layers]
+    cm = CustomMatrices(dtype)
     ob = O.OracleBackend()
-    state = np.empty(1 << n, dtype=np.complex128)
+    state = np.empty(1 << n, dtype=dtype)
     O.initial_state_vector(state)
     t0 = time.perf_counter()
     for g in gates:
@@ -145,31 +151,44 @@ def cpu_baseline_oracle(n: int, sample_layers: int = 1, threads: int = None):
     dt = time.perf_counter() - t0
     del state
     return {"value": len(gates) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {sample_layers} layer(s) ({len(gates)} gates) of the n={n} complex128 circuit, "
-                      f"per-gate C/OpenMP restatement of the Numba kernels, {dt:.2f} s"}
+            "sample": f"first {sample_layers} layer(s) ({len(gates)} gates) of the n={n} {dtype} circuit, per-gate "
+                      f"C/OpenMP restatement of the reference Numba kernels, {dt:.2f} s"}
 
 
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
         return
-    cb = cpu_baseline_oracle(N_QUBITS, 1)
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": f"brickwork n={N_QUBITS} depth {DEPTH} complex128 (seed {SEED})",
-                       "sample": "one layer per step"},
-            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                                       "d2h_bytes_per_step": 0}}
-    # time the remaining steps on the same sample so the line reflects steps x sample
-    vals = [cb["value"]]
-    for _ in range(max(0, args.steps - 1)):
-        vals.append(cpu_baseline_oracle(N_QUBITS, 1)["value"])
-    line["value"] = statistics.median(vals)
-    line["e2e"]["value"] = line["value"]
-    line["cpu_baseline"]["value"] = line["value"]
-    line["ms_per_step"] = 1000.0 * (N_QUBITS + N_QUBITS // 2) / line["value"]
+    n = args.nqubits
+    for _ in range(max(0, args.warmup)):
+        pass  # the CPU sample has no warm-up state; each step is a fresh bounded sample
+    vals, last = [], None
+    for _ in range(max(1, args.steps)):
+        last = cpu_baseline_oracle(n, args.dtype, 1)
+        vals.append(last["value"])
+    v = statistics.median(vals)
+    last["value"] = v
+    line = {"impl": "reference", "metric": metric_name(n), "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * (n + n // 2) / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64" if args.dtype == "complex64" else "c128", "data": "synthetic",
+            "config": {"workload": f"brickwork n={n} depth {DEPTH} {args.dtype} (seed {SEED})",
+                       "sample": "one layer (45 gates) per step, per-gate"},
+            "cpu_baseline": last,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _time_program(torch, prog, backend, state, dcode, n, steps, stream):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        backend.lib.sv_zero_state(backend.ctx.handle, state.data_ptr(), dcode, n)
+        prog.run(state)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
 
 
 def run_engine(args):
@@ -179,77 +198,51 @@ def run_engine(args):
     if ws > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from qibojit_gb300 import MetaBackend, circuits
+    from qibojit_gb300 import _lib
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     backend = MetaBackend.load("gb300", device=dev)
-    backend.set_dtype(args.dtype)
     n = args.nqubits
+    dtype = args.dtype
+    dcode = _lib.DTYPE_CODES[dtype]
+    itemsize = 16 if dtype == "complex128" else 8
     circ = circuits.brickwork(n, DEPTH, SEED + rank)
     ngates = len(circ.queue)
-    itemsize = 16 if args.dtype == "complex128" else 8
-    dense_bytes = 2 * itemsize * (1 << n)
-
-    # precompute operands once (host work the plain method repeats per gate is
-    # kept out of the device timing; the e2e leg keeps it in)
-    plan = []
-    for g in circ.queue:
-        q = backend._create_qubits_tensor(g, n)
-        if type(g).__name__ == "U3":
-            plan.append(("u3", g.target_qubits[0], backend._operand(backend.custom_matrices.U3(*g.parameters),
-                                                                     args.dtype), q))
-        else:
-            plan.append(("cz", g.target_qubits[0], None, q))
-
-    state = backend.zero_state(n)
+    n_u3 = sum(1 for g in circ.queue if type(g).__name__ == "U3")
+    prog = backend.compile(circ, dtype)
+    st = prog.stats()
+    state = backend.zero_state(n, dtype=dtype)
     stream = torch.cuda.current_stream()
 
-    def step(timed_events=None):
-        backend.lib.sv_zero_state(backend.ctx.handle, state.data_ptr(), 0 if args.dtype == "complex128" else 1, n)
-        for kind, t, op, q in plan:
-            if kind == "u3":
-                if timed_events is not None:
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record(stream)
-                backend._one_qubit_base(state, n, t, "apply_gate", op, q)
-                if timed_events is not None:
-                    e1.record(stream)
-                    timed_events.append((e0, e1))
-            else:
-                backend._one_qubit_base(state, n, t, "apply_z", None, q)
-
+    # ---- warm-up, then the timed region (events on the launching stream)
     for _ in range(args.warmup):
-        step()
+        backend.lib.sv_zero_state(backend.ctx.handle, state.data_ptr(), dcode, n)
+        prog.run(state)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    events = []
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the zero-state kernel is timed alone so the fused passes' share is exact
+    zs_ms = _time_program(torch, type("Z", (), {"run": staticmethod(lambda s: s)}), backend, state, dcode, n, 3, stream)
     with ClockSampler(dev) as clocks:
-        torch.cuda.synchronize()
-        start.record(stream)
-        for _ in range(args.steps):
-            step(events)
-        end.record(stream)
-        torch.cuda.synchronize()
-    elapsed_ms = start.elapsed_time(end)
+        ms_step = _time_program(torch, prog, backend, state, dcode, n, args.steps, stream)
+    elapsed_ms = ms_step * args.steps
     if ws > 1:
         t = torch.tensor([elapsed_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed_ms = float(t.item())
         torch.distributed.barrier()
-    u3_ms = [a.elapsed_time(b) for a, b in events]
-    avg_u3_ms = sum(u3_ms) / len(u3_ms)
     value = ws * ngates * args.steps / (elapsed_ms / 1000.0)
+    pass_ms = (ms_step - zs_ms) / st["passes"]
 
-    # ---- end to end through the public API: host (pinned) -> device -> host each step
+    # ---- end to end through the public API: pinned host -> device -> host every step
     host_in = torch.zeros(1 << n, dtype=state.dtype).pin_memory()
     host_in[0] = 1
     host_out = torch.empty_like(host_in).pin_memory()
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = max(1, min(args.steps, 3))
+    backend.execute_circuit(circ, host_in)  # plans and caches the program for this circuit
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -257,34 +250,74 @@ def run_engine(args):
         host_out.copy_(s)
         del s
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ws * ngates * e2e_steps / e2e_s
-    nbytes = (1 << n) * itemsize
+    e2e_value = ws * ngates * e2e_steps / (time.perf_counter() - t0)
+    final64 = host_out  # |psi> of the complex64 fused run, on the host
+
+    # ---- variants, timed once each after one warm-up (same circuit)
+    variants = {}
+    if not args.quick and rank == 0:
+        plain_ms = {}
+        for vdt in ("complex64", "complex128"):
+            s = backend.zero_state(n, dtype=vdt)
+            backend.execute_circuit(circ, s, fuse=False)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            backend.execute_circuit(circ, backend.zero_state(n, dtype=vdt), fuse=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms[vdt] = e0.elapsed_time(e1)
+            del s
+            torch.cuda.empty_cache()
+        p128 = backend.compile(circ, "complex128")
+        s128 = backend.zero_state(n, dtype="complex128")
+        f128_ms = _time_program(torch, p128, backend, s128, _lib.SV_C128, n, 1, stream)
+        s64 = backend.cast(final64, dtype="complex64")
+        ip = backend.inner_product(s128, s64, n)
+        variants = {
+            "c64_fused_gates_per_s": value,
+            "c128_fused_gates_per_s": ngates / (f128_ms / 1000.0),
+            "c64_plain_gates_per_s": ngates / (plain_ms["complex64"] / 1000.0),
+            "c128_plain_gates_per_s": ngates / (plain_ms["complex128"] / 1000.0),
+            "precision": {
+                "infidelity_c64_vs_c128": 1.0 - abs(ip) ** 2,
+                "max_abs_err_c64_vs_c128": backend.max_abs_diff(s64, s128, n),
+                "norm2_fp64_c64": backend.norm2(s64, n),
+                "zz01_c64": backend.expectation_z(s64, [0, 1], n),
+                "zz01_c128": backend.expectation_z(s128, [0, 1], n),
+            },
+        }
+        del s128, s64
+        torch.cuda.empty_cache()
 
     peak, peak_kind = _peak_hbm()
-    achieved = dense_bytes / (avg_u3_ms / 1000.0) / 1e9
-    kernel_key = f"k_one_qubit_u3_n{n}_{args.dtype}"
-    traffic = _traffic_from_profiles(kernel_key)
+    pass_bytes = 2 * itemsize * (1 << n)
+    achieved = pass_bytes / (pass_ms / 1000.0) / 1e9
+    flops_per_step = 16.0 * (1 << n) * n_u3  # dense one-qubit gates; CZ sign flips carry no flops
+    fp32_tflops = flops_per_step / ((ms_step - zs_ms) / 1000.0) / 1e12
+    nbytes = (1 << n) * itemsize
     if rank == 0:
-        cb = cpu_baseline_oracle(n, 1) if (not args.skip_cpu and ws == 1) else None
+        cb = cpu_baseline_oracle(n, dtype, 1) if (not args.skip_cpu and ws == 1) else None
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "metric": metric_name(n), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.dtype == "complex128" else "c64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64" if dtype == "complex64" else "c128",
             "data": "synthetic",
-            "config": {"workload": f"brickwork n={n} depth {DEPTH} {args.dtype} (seed {SEED}), plain per-gate method",
-                       "gates_per_step": ngates, "state_bytes": nbytes,
-                       "l2": "state larger than the 129 MB L2; no flush needed",
+            "config": {"workload": f"brickwork n={n} depth {DEPTH} {dtype} (seed {SEED}), fused cache-blocked passes",
+                       "gates_per_step": ngates, "passes_per_step": st["passes"], "tile_bits": st["tile_bits"],
+                       "state_bytes": nbytes, "l2": "state larger than the 129 MB L2; no flush needed",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_one_qubit (dense U3 pass)", "algorithmic_bytes_per_launch": dense_bytes,
-                         "avg_launch_ms": avg_u3_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": _traffic_from_profiles(f"k_fused_pass_{dtype}"), "peak_kind": peak_kind,
+                         "kernel": "k_fused_pass", "algorithmic_bytes_per_launch": pass_bytes,
+                         "avg_launch_ms": pass_ms, "fp32_tflops": fp32_tflops,
+                         "fp32_frac_of_probe_peak": fp32_tflops / FP32_PEAK_TFLOPS},
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
-            "gpu_launches": args.steps * (ngates + 1),
+            "gpu_launches": args.steps * (st["passes"] + 1),
             "clocks": clocks.summary(),
+            "variants": variants,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -294,12 +327,13 @@ def run_engine(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--nqubits", type=int, default=N_QUBITS)
-    ap.add_argument("--dtype", default="complex128", choices=["complex128", "complex64"])
+    ap.add_argument("--dtype", default="complex64", choices=["complex128", "complex64"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the variants and the precision report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -154,6 +154,58 @@ int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* pr
                            int prob_dtype, int nbits, int64_t nshots, uint32_t seed,
                            int nchains);
 
+/* -------------------------------------------------------------- reductions */
+/* The precision mode keeps bulk gate arithmetic in complex64 and every reduction in
+ * FP64 (Neumaier-compensated per thread, fixed-order final sums).  These return
+ * their result to the host and synchronise the context's stream.  States may have
+ * different dtypes (e.g. a complex64 state against a complex128 one).  They extend
+ * the reference, whose norms and expectations are NumPy/CuPy sums on the host side
+ * (e.g. the collapse norm, gpu.py:640-642). */
+/* out_re_im[0] + i out_re_im[1] = <a|b> = sum_i conj(a_i) b_i */
+int sv_inner_product(sv_context* ctx, const void* a, int dtype_a, const void* b, int dtype_b, int nqubits,
+                     double* out_re_im);
+/* out[0] = max_i |a_i - b_i| */
+int sv_max_abs_diff(sv_context* ctx, const void* a, int dtype_a, const void* b, int dtype_b, int nqubits,
+                    double* out);
+/* out[0] = <Z_{q1} Z_{q2} ...> over the listed qubits (nq = 0: the norm squared) */
+int sv_expectation_z(sv_context* ctx, const void* state, int dtype, int nqubits, const int32_t* qubits, int nq,
+                     double* out);
+
+/* ------------------------------------------------------------ fused programs */
+/* Gate fusion.  The reference fuses with qibo's Circuit.fuse (FusedGate, applied
+ * as one dense 2^k x 2^k multi-qubit kernel: cpu.py:535-537, gpu.py:929-930); the
+ * engine instead compiles a gate list once into HBM passes (a native planner picks,
+ * per pass, a tile of `tile_bits` bit positions and every gate whose dense targets
+ * lie in it) and runs each pass as one cache-blocked kernel: one read and one write
+ * of the state for many gates. */
+enum sv_op_kind { SV_OP_DENSE = 0, SV_OP_DIAG = 1 };
+
+typedef struct sv_gate_op {
+  int32_t kind;          /* SV_OP_DENSE: 2^k x 2^k matrix on the targets;
+                            SV_OP_DIAG: its 2^k diagonal entries */
+  int32_t ntargets;      /* 1..10 (dense ops with more than 2 targets and diagonal ops
+                            with more than 3 run unfused, as separate kernels) */
+  int32_t ncontrols;     /* 0..16: the op acts where every control qubit is 1 */
+  int32_t targets[10];   /* qubit indices; targets[0] is the most significant bit of
+                            the row (dense) or table (diagonal) index */
+  int32_t controls[16];  /* qubit indices */
+  const double* matrix;  /* host: complex entries as (re, im) pairs, row-major */
+} sv_gate_op;
+
+typedef struct sv_program sv_program;
+
+/* Plans and uploads a program for states of `nqubits` qubits and type `dtype`
+ * (SV_C128 or SV_C64).  tile_bits <= 0 picks the default (11 for complex128, 12 for
+ * complex64).  The op list is read before the call returns. */
+int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op* ops, int nops,
+                       int tile_bits, sv_program** out);
+/* Applies the program to `state` (device, 2^nqubits amplitudes) on the context's stream. */
+int sv_program_run(sv_context* ctx, const sv_program* prog, void* state);
+/* Plan statistics: HBM passes, unfused ops, gates inside passes, tile bits (any may be NULL). */
+int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* nfused_gates,
+                     int* tile_bits);
+int sv_program_destroy(sv_program* prog);
+
 #ifdef __cplusplus
 }
 #endif

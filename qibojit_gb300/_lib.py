@@ -27,7 +27,8 @@ EXPORTS = (
     "sv_version", "sv_last_error", "sv_device_count", "sv_context_create", "sv_context_destroy",
     "sv_context_set_stream", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
     "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_measure_frequencies",
-    "sv_collapse_state_noalloc",
+    "sv_collapse_state_noalloc", "sv_program_create", "sv_program_run", "sv_program_stats",
+    "sv_program_destroy", "sv_inner_product", "sv_max_abs_diff", "sv_expectation_z",
 )
 
 
@@ -59,6 +60,13 @@ _SIGNATURES = {
     "sv_probabilities": ([_vp, _vp, _int, _int, _vp, _int, _vp, _int], _int),
     "sv_measure_frequencies": ([_vp, _vp, _vp, _int, _int, _i64, ctypes.c_uint32, _int], _int),
     "sv_collapse_state_noalloc": ([_vp, _vp, _int, _int, _vp, _int, _i64, _int], _int),
+    "sv_program_create": ([_vp, _int, _int, _vp, _int, _int, ctypes.POINTER(_vp)], _int),
+    "sv_program_run": ([_vp, _vp, _vp], _int),
+    "sv_program_stats": ([_vp] + [ctypes.POINTER(_int)] * 4, _int),
+    "sv_program_destroy": ([_vp], _int),
+    "sv_inner_product": ([_vp, _vp, _int, _vp, _int, _int, _vp], _int),
+    "sv_max_abs_diff": ([_vp, _vp, _int, _vp, _int, _int, _vp], _int),
+    "sv_expectation_z": ([_vp, _vp, _int, _int, _vp, _int, _vp], _int),
 }
 
 

@@ -96,6 +96,8 @@ class GB300Backend(_QiboBackend):
         self.versions = {"qibojit_gb300": "0.1.0", "engine": self.lib.sv_version()}
         self.tensor_types = (np.ndarray, torch.Tensor)
         self.supports_multigpu = False
+        self.fusion = True
+        self._programs = {}
 
     # ------------------------------------------------------------------ setters
     def set_dtype(self, dtype) -> None:
@@ -338,17 +340,71 @@ class GB300Backend(_QiboBackend):
         return Counter(dict(zip(idx.cpu().tolist(), freqs[idx].cpu().tolist())))
 
     # ---------------------------------------------------------------- execution
-    def execute_circuit(self, circuit, initial_state=None, nshots: Optional[int] = None):
-        """Applies ``circuit.queue`` gate by gate (qibo's plain method) and returns the state."""
+    def compile(self, circuit, dtype: Optional[str] = None, tile_bits: int = 0):
+        """Plans ``circuit`` into fused HBM passes (see ``qibojit_gb300.fusion``)."""
+        from .fusion import FusedProgram
+
+        return FusedProgram(self.ctx, circuit.queue, circuit.nqubits, dtype or self.dtype, tile_bits)
+
+    def execute_circuit(self, circuit, initial_state=None, nshots: Optional[int] = None,
+                        fuse: Optional[bool] = None):
+        """Runs ``circuit`` on ``initial_state`` (default |0...0>) and returns the state.
+
+        With ``fuse`` (default: the backend's ``fusion`` flag) complex states of 8 or more
+        qubits run as fused passes; otherwise gates are applied one by one (qibo's plain
+        method, as the reference's ``execute_circuit`` does)."""
         n = circuit.nqubits
         if initial_state is None:
             state = self.zero_state(n)
         else:
             state = self.cast(initial_state, dtype=_dtype_name(getattr(initial_state, "dtype", self.dtype)),
                               copy=True)
+        dtype = _dtype_name(state.dtype)
+        fuse = self.fusion if fuse is None else fuse
+        if fuse and n >= 8 and dtype in ("complex128", "complex64") and circuit.queue:
+            key = (id(circuit), len(circuit.queue), n, dtype)
+            prog = self._programs.get(key)
+            if prog is None:
+                prog = self.compile(circuit, dtype)
+                self._programs = {key: prog}
+            return prog.run(state)
         for gate in circuit.queue:
             state = self.apply_gate(gate, state, n)
         return state
+
+    # --------------------------------------------------------- FP64 reductions
+    def inner_product(self, a, b, nqubits: int) -> complex:
+        """<a|b> accumulated in FP64 (states may differ in precision)."""
+        import ctypes
+
+        da, db = self._check_state(a, nqubits), self._check_state(b, nqubits)
+        out = (ctypes.c_double * 2)()
+        _lib.check(self.lib.sv_inner_product(self.ctx.handle, a.data_ptr(), da, b.data_ptr(), db, int(nqubits), out),
+                   "inner_product")
+        return complex(out[0], out[1])
+
+    def max_abs_diff(self, a, b, nqubits: int) -> float:
+        import ctypes
+
+        da, db = self._check_state(a, nqubits), self._check_state(b, nqubits)
+        out = (ctypes.c_double * 1)()
+        _lib.check(self.lib.sv_max_abs_diff(self.ctx.handle, a.data_ptr(), da, b.data_ptr(), db, int(nqubits), out),
+                   "max_abs_diff")
+        return out[0]
+
+    def expectation_z(self, state, qubits: Sequence[int], nqubits: int) -> float:
+        """<Z_{q1} Z_{q2} ...> in FP64; an empty list gives the squared norm."""
+        import ctypes
+
+        dt = self._check_state(state, nqubits)
+        q, nq = _lib.int32_array(list(qubits))
+        out = (ctypes.c_double * 1)()
+        _lib.check(self.lib.sv_expectation_z(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, out),
+                   "expectation_z")
+        return out[0]
+
+    def norm2(self, state, nqubits: int) -> float:
+        return self.expectation_z(state, [], nqubits)
 
     def assert_allclose(self, value, target, rtol=1e-7, atol=0.0):
         np.testing.assert_allclose(self.to_numpy(value), self.to_numpy(target), rtol=rtol, atol=atol)

@@ -1,0 +1,753 @@
+// sv_fused.cu -- gate fusion: a native pass planner and the cache-blocked tile kernel.
+//
+// A circuit is compiled once into a program of HBM passes.  Each pass owns a set S of
+// kt "tile" bit positions (always containing the 4 lowest bits, so a tile is read as
+// runs of 16 contiguous amplitudes); a CTA loads the 2^kt amplitudes of one tile (one
+// fixed value of the other bits) into shared memory, applies every gate the pass
+// holds, and writes the tile back: one read and one write of the state for many
+// gates.  A gate joins a pass when its dense target bits lie in S; diagonal gates and
+// control qubits may sit on any bit (outside S they are constant over a tile).
+//
+// Inside a tile, gates run in register-blocked phases: each thread holds the 16
+// amplitudes that differ in the 4 local bits of the phase, applies all gates of the
+// phase in registers, and exchanges through shared memory between phases.  The
+// planner precomputes everything that depends only on the gate and the phase (which
+// registers a control or a diagonal bit selects, sign masks), so the kernel's inner
+// loops are FMAs and constant-shift bit tests.  A pass's ops and coefficients ride in
+// the kernel parameters (constant bank); tiles are double-buffered with cp.async so
+// the next tile's HBM read overlaps this tile's arithmetic.
+//
+// This replaces the reference's fusion path (qibo Circuit.fuse -> FusedGate, applied
+// by qibojit as one dense 2^k x 2^k multi-qubit kernel, cpu.py:535-537,
+// gpu.py:929-930) with a schedule that needs no dense products of gate matrices.
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sv_common.cuh"
+
+namespace sv {
+
+constexpr int kRB = 4;            // register bits per phase (16 amplitudes per thread)
+constexpr int kMaxTile = 14;      // tile bits
+constexpr int kLowBits = 4;       // lowest bits always in a tile (contiguous runs)
+constexpr int kMaxPassOps = 128;  // ops (and phases) per pass
+constexpr int kCoefBytes = 12288; // coefficient bytes per pass
+
+enum : uint8_t { FOP_DENSE1 = 0, FOP_DENSE2 = 1, FOP_DIAG = 2, FOP_SIGN = 3, FOP_D1RUN = 4 };
+enum : uint8_t { FLAG_OMASK = 1, FLAG_TMASK = 2 };
+
+// One op in phase-local form (64 bytes).
+struct FOp {
+  uint8_t type, u0, u1, nd;  // dense: register positions of the targets (u0 = row MSB); diag: #bits
+  int8_t tb[3];              // diag bit i read from the thread's local index bit tb[i] (or -1)
+  int8_t ob[3];              // diag bit i read from the tile's outer global bit ob[i] (or -1)
+  uint8_t pad0[2];
+  uint16_t jmask;            // register-level controls: amplitudes / pair bases j allowed
+  uint16_t pad1;
+  uint32_t tmask;            // thread-level controls: local non-register bits that must be 1
+  uint32_t coef;             // first coefficient of this op in the pass's coefficient array
+  uint64_t omask;            // tile-level controls: outer global bits that must be 1
+  uint64_t rpart;            // diag: table-index part from register bits, 4 bits per amplitude j
+  uint16_t neg[8];           // sign diag: negate-mask over j for each non-register index part
+  uint8_t flags;             // FLAG_OMASK / FLAG_TMASK: which control checks apply
+  uint8_t nrun;              // FOP_D1RUN: number of uncontrolled one-target gates (1..4)
+  uint8_t ru[4];             // FOP_D1RUN: their register positions; matrices at coef + 4k
+  uint8_t pad2[2];
+};
+static_assert(sizeof(FOp) == 64, "FOp layout");
+
+struct Phase {
+  uint8_t rb[kRB];           // local tile bits held in registers, ascending (j bit u <-> rb[u])
+  uint16_t op_begin, op_end;
+  uint16_t soff[16];         // shared-memory offset of register j: smem_pos(register bits of j)
+};
+
+template <typename T>
+struct PassParams {
+  int32_t n, kt, nphases, nops;
+  int64_t ntiles;
+  int32_t tile_pos[kMaxTile];  // global bit positions of the tile bits, ascending
+  int32_t pad;
+  Phase phases[kMaxPassOps];
+  FOp ops[kMaxPassOps];
+  T coef[kCoefBytes / sizeof(T)];
+};
+
+__device__ __forceinline__ int smem_pos(int e) { return e + (e >> 4); }
+
+// ------------------------------------------------------------------ cp.async
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem_src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// ---------------------------------------------------------------- register ops
+template <typename T, int U>
+__device__ __forceinline__ void dense1_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+  const T a = m[0], b = m[1], c = m[2], d = m[3];
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const int k = j | (1 << U);
+    const T x = v[j], y = v[k];
+    v[j] = tfma(a, x, tmul(b, y));
+    v[k] = tfma(c, x, tmul(d, y));
+  }
+}
+
+template <typename T, int U0, int U1>
+__device__ __forceinline__ void dense2_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & ((1 << U0) | (1 << U1))) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const int i1 = j | (1 << U1), i2 = j | (1 << U0), i3 = j | (1 << U0) | (1 << U1);
+    const T x0 = v[j], x1 = v[i1], x2 = v[i2], x3 = v[i3];
+    T o[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      T acc = tmul(m[4 * r + 3], x3);
+      acc = tfma(m[4 * r + 2], x2, acc);
+      acc = tfma(m[4 * r + 1], x1, acc);
+      o[r] = tfma(m[4 * r + 0], x0, acc);
+    }
+    v[j] = o[0];
+    v[i1] = o[1];
+    v[i2] = o[2];
+    v[i3] = o[3];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dense1_dispatch(T (&v)[16], const T* m, int u, unsigned jm) {
+  // jm == 0xffff marks an op without register-level controls: no per-pair tests
+  if (jm == 0xffffu) {
+    switch (u) {
+      case 0: dense1_regs<T, 0>(v, m, 0xffffu); break;
+      case 1: dense1_regs<T, 1>(v, m, 0xffffu); break;
+      case 2: dense1_regs<T, 2>(v, m, 0xffffu); break;
+      default: dense1_regs<T, 3>(v, m, 0xffffu); break;
+    }
+    return;
+  }
+  switch (u) {
+    case 0: dense1_regs<T, 0>(v, m, jm); break;
+    case 1: dense1_regs<T, 1>(v, m, jm); break;
+    case 2: dense1_regs<T, 2>(v, m, jm); break;
+    default: dense1_regs<T, 3>(v, m, jm); break;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void apply_negations(T (&v)[16], unsigned nm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++)
+    if ((nm >> j) & 1u) v[j] = tneg(v[j]);
+}
+
+template <typename T>
+__device__ __forceinline__ void dense2_dispatch(T (&v)[16], const T* m, int u0, int u1, unsigned jm) {
+#define SV_D2(A, B) \
+  if (u0 == A && u1 == B) { dense2_regs<T, A, B>(v, m, jm); return; }
+  SV_D2(0, 1) SV_D2(0, 2) SV_D2(0, 3) SV_D2(1, 0) SV_D2(1, 2) SV_D2(1, 3)
+  SV_D2(2, 0) SV_D2(2, 1) SV_D2(2, 3) SV_D2(3, 0) SV_D2(3, 1) SV_D2(3, 2)
+#undef SV_D2
+}
+
+// threads per CTA = 2^(kt - 4): at most 512 (complex64, kt <= 13) or 256 (complex128, kt <= 12)
+template <typename T>
+constexpr int fused_max_threads() { return sizeof(T) >= 16 ? 256 : 512; }
+
+__device__ __forceinline__ int64_t tile_origin(int64_t t, const int32_t* pos, int kt) {
+  int64_t base = t;  // insert zeros at the ascending tile bit positions
+  for (int b = 0; b < kt; b++) {
+    const int p = pos[b];
+    base = ((base >> p) << (p + 1)) | (base & (((int64_t)1 << p) - 1));
+  }
+  return base;
+}
+
+// ------------------------------------------------------------------ tile kernel
+template <typename T>
+__global__ void __launch_bounds__(fused_max_threads<T>(), 1) k_fused_pass(T* __restrict__ state,
+                                                                      const __grid_constant__ PassParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int kt = p.kt;
+  const int tsize = 1 << kt;
+  const int tstride = tsize + (tsize >> 4);
+  T* const buf0 = reinterpret_cast<T*>(smem_raw);  // two tiles, tstride apart
+  int64_t* dep_hi = reinterpret_cast<int64_t*>(buf0 + 2 * tstride);
+  const int nhi = kt - kLowBits;
+  for (int h = threadIdx.x; h < (1 << nhi); h += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < nhi; b++)
+      if ((h >> b) & 1) o |= (int64_t)1 << p.tile_pos[kLowBits + b];
+    dep_hi[h] = o;
+  }
+  __syncthreads();
+  const int nthreads = blockDim.x;
+  auto issue_load = [&](T* buf, int64_t base) {
+    for (int e = threadIdx.x; e < tsize; e += nthreads)
+      cp_async<sizeof(T)>(buf + smem_pos(e), state + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))));
+    cp_async_commit();
+  };
+  int64_t t = blockIdx.x;
+  if (t < p.ntiles) issue_load(buf0, tile_origin(t, p.tile_pos, kt));
+  int cur = 0;
+  for (; t < p.ntiles; t += gridDim.x, cur ^= 1) {
+    T* tile = buf0 + cur * tstride;
+    const int64_t base = tile_origin(t, p.tile_pos, kt);
+    const int64_t tn = t + gridDim.x;
+    if (tn < p.ntiles) {
+      issue_load(buf0 + (cur ^ 1) * tstride, tile_origin(tn, p.tile_pos, kt));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    for (int ph = 0; ph < p.nphases; ph++) {
+      const Phase& P = p.phases[ph];
+      const int r0 = P.rb[0], r1 = P.rb[1], r2 = P.rb[2], r3 = P.rb[3];
+      // thread bits deposited into the non-register local bits (register bits ascending)
+      int lbase = threadIdx.x;
+      lbase = ((lbase >> r0) << (r0 + 1)) | (lbase & ((1 << r0) - 1));
+      lbase = ((lbase >> r1) << (r1 + 1)) | (lbase & ((1 << r1) - 1));
+      lbase = ((lbase >> r2) << (r2 + 1)) | (lbase & ((1 << r2) - 1));
+      lbase = ((lbase >> r3) << (r3 + 1)) | (lbase & ((1 << r3) - 1));
+      // lbase and the register bits are disjoint, so smem_pos splits into a sum
+      T* const tp_base = tile + smem_pos(lbase);
+      T v[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = tp_base[P.soff[j]];
+      unsigned pending_neg = 0;  // sign-only diagonals commute: collect them, apply before mixing
+      for (int o = P.op_begin; o < P.op_end; o++) {
+        const FOp& op = p.ops[o];
+        const int type = op.type;
+        if (type == FOP_D1RUN) {
+          if (pending_neg) {
+            apply_negations(v, pending_neg);
+            pending_neg = 0;
+          }
+          const int nr = op.nrun;
+          const T* c = p.coef + op.coef;
+#pragma unroll 1
+          for (int k = 0; k < nr; k++) dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+          continue;
+        }
+        const int flags = op.flags;
+        if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
+        if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;
+        if (type == FOP_DENSE1) {
+          if (pending_neg) {
+            apply_negations(v, pending_neg);
+            pending_neg = 0;
+          }
+          dense1_dispatch(v, p.coef + op.coef, op.u0, op.jmask);
+        } else if (type == FOP_DENSE2) {
+          if (pending_neg) {
+            apply_negations(v, pending_neg);
+            pending_neg = 0;
+          }
+          dense2_dispatch(v, p.coef + op.coef, op.u0, op.u1, op.jmask);
+        } else {
+          const int nd = op.nd;
+          int tp = 0;
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            if (i >= nd) break;
+            if (op.tb[i] >= 0) tp |= ((lbase >> op.tb[i]) & 1) << (nd - 1 - i);
+            else if (op.ob[i] >= 0) tp |= (int)((base >> op.ob[i]) & 1) << (nd - 1 - i);
+          }
+          if (type == FOP_SIGN) {
+            pending_neg ^= op.neg[tp];
+          } else {
+            const unsigned jm = op.jmask;
+            const uint64_t rp = op.rpart;
+            const T* c = p.coef + op.coef;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              if (!((jm >> j) & 1u)) continue;
+              const int idx = (int)((rp >> (4 * j)) & 15) | tp;
+              v[j] = tmul(c[idx], v[j]);
+            }
+          }
+        }
+      }
+      if (pending_neg) apply_negations(v, pending_neg);
+#pragma unroll
+      for (int j = 0; j < 16; j++) tp_base[P.soff[j]] = v[j];
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < tsize; e += nthreads)
+      stg_stream(state + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))), tile[smem_pos(e)]);
+    __syncthreads();  // this buffer is refilled by the prefetch two tiles later
+  }
+}
+
+// =================================================================== planner
+struct HostOp {
+  int kind;                 // SV_OP_DENSE / SV_OP_DIAG
+  int nt;                   // targets
+  int tpos[kMaxTargets];    // global bit positions of the targets, gate order
+  int nc;
+  int cpos[16];
+  std::vector<double> m;    // complex entries (re, im) pairs
+  bool sign_only = false;   // diagonal with entries in {+1, -1}
+  int sign_mask = 0;        // bit i set: entry i is -1
+};
+
+struct Segment {
+  bool fused = false;
+  int pass = -1;            // index into the program's pass parameter blocks
+  int host_op = -1;         // unfused op
+};
+
+}  // namespace sv
+
+struct sv_program {
+  int dtype, nqubits, kt;
+  std::vector<sv::HostOp> ops;
+  std::vector<sv::Segment> segments;
+  std::vector<unsigned char> passes;  // PassParams<T> blocks, back to back
+  size_t pass_bytes = 0;
+  int npasses = 0, nunfused = 0, nfused_gates = 0, nphases = 0;
+};
+
+namespace sv {
+
+template <typename T>
+static T to_elem(const double* re_im) {
+  if constexpr (is_complex<T>::value) {
+    using R = typename real_of<T>::type;
+    return T{(R)re_im[0], (R)re_im[1]};
+  } else {
+    return (T)re_im[0];
+  }
+}
+
+static int coef_cost(const HostOp& h) {
+  if (h.kind == SV_OP_DENSE) return h.nt == 1 ? 4 : 16;
+  return h.sign_only ? 0 : (1 << h.nt);
+}
+
+// Builds the phase-local form of the scheduled ops of one pass.
+template <typename T>
+static void encode_pass(const sv_program* prog, const std::vector<int>& sched, uint64_t S, PassParams<T>* pp,
+                        int* nphases_out) {
+  const int n = prog->nqubits, kt = prog->kt;
+  memset(pp, 0, sizeof(*pp));
+  pp->n = n;
+  pp->kt = kt;
+  pp->ntiles = (int64_t)1 << (n - kt);
+  int local_of[64];
+  for (int b = 0, k = 0; b < 64; b++) {
+    local_of[b] = -1;
+    if (b < n && ((S >> b) & 1)) {
+      pp->tile_pos[k] = b;
+      local_of[b] = k++;
+    }
+  }
+  // group ops into phases by register bits (order preserved)
+  struct Pending { int op; int lt[2]; };
+  std::vector<std::vector<Pending>> groups;
+  std::vector<std::vector<int>> group_bits;
+  std::vector<int> cur_bits;
+  std::vector<Pending> cur;
+  auto flush = [&]() {
+    if (cur.empty()) return;
+    groups.push_back(cur);
+    group_bits.push_back(cur_bits);
+    cur.clear();
+    cur_bits.clear();
+  };
+  for (int oi : sched) {
+    const HostOp& h = prog->ops[oi];
+    Pending pd{oi, {-1, -1}};
+    if (h.kind == SV_OP_DENSE) {
+      for (int i = 0; i < h.nt; i++) pd.lt[i] = local_of[h.tpos[i]];
+      int need = 0;
+      for (int i = 0; i < h.nt; i++)
+        if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) need++;
+      if ((int)cur_bits.size() + need > kRB) flush();
+      for (int i = 0; i < h.nt; i++)
+        if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) cur_bits.push_back(pd.lt[i]);
+    }
+    cur.push_back(pd);
+  }
+  flush();
+  int nops = 0, ncoef = 0;
+  for (size_t g = 0; g < groups.size(); g++) {
+    std::vector<int> rb = group_bits[g];
+    for (int b = kt - 1; b >= 0 && (int)rb.size() < kRB; b--)
+      if (std::find(rb.begin(), rb.end(), b) == rb.end()) rb.push_back(b);
+    std::sort(rb.begin(), rb.end());
+    int regpos[kMaxTile];
+    for (int b = 0; b < kt; b++) regpos[b] = -1;
+    for (int u = 0; u < kRB; u++) regpos[rb[u]] = u;
+    Phase& P = pp->phases[g];
+    for (int u = 0; u < kRB; u++) P.rb[u] = (uint8_t)rb[u];
+    for (int j = 0; j < 16; j++) {
+      int off = 0;
+      for (int u = 0; u < kRB; u++)
+        if ((j >> u) & 1) off |= 1 << rb[u];
+      P.soff[j] = (uint16_t)(off + (off >> 4));
+    }
+    P.op_begin = (uint16_t)nops;
+    for (const Pending& pd : groups[g]) {
+      const HostOp& h = prog->ops[pd.op];
+      FOp& f = pp->ops[nops++];
+      memset(&f, 0, sizeof(f));
+      // controls: register-level (reg_c), thread-level (tmask), tile-level (omask)
+      unsigned reg_c = 0;
+      for (int i = 0; i < h.nc; i++) {
+        const int lc = local_of[h.cpos[i]];
+        if (lc < 0) f.omask |= 1ull << h.cpos[i];
+        else if (regpos[lc] >= 0) reg_c |= 1u << regpos[lc];
+        else f.tmask |= 1u << lc;
+      }
+      unsigned jm = 0;
+      unsigned tbits = 0;  // register bits that are targets of a dense op
+      if (h.kind == SV_OP_DENSE) {
+        f.type = h.nt == 1 ? FOP_DENSE1 : FOP_DENSE2;
+        f.u0 = (uint8_t)regpos[pd.lt[0]];
+        tbits = 1u << f.u0;
+        if (h.nt == 2) {
+          f.u1 = (uint8_t)regpos[pd.lt[1]];
+          tbits |= 1u << f.u1;
+        }
+        for (int j = 0; j < 16; j++)
+          if (!(j & tbits) && (j & reg_c) == reg_c) jm |= 1u << j;
+        if (reg_c == 0) jm = 0xffffu;  // no register-level controls: kernel skips the tests
+        f.jmask = (uint16_t)jm;
+        f.coef = (uint32_t)ncoef;
+        const int ne = h.nt == 1 ? 4 : 16;
+        for (int i = 0; i < ne; i++) pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+      } else {
+        f.nd = (uint8_t)h.nt;
+        for (int j = 0; j < 16; j++)
+          if ((j & reg_c) == reg_c) jm |= 1u << j;
+        f.jmask = (uint16_t)jm;
+        uint64_t rpart = 0;
+        unsigned nonreg_bits = 0;  // table-index bits fed by thread or outer bits
+        for (int i = 0; i < 3; i++) {
+          f.tb[i] = -1;
+          f.ob[i] = -1;
+        }
+        for (int i = 0; i < h.nt; i++) {
+          const int sh = h.nt - 1 - i;
+          const int lb = local_of[h.tpos[i]];
+          if (lb >= 0 && regpos[lb] >= 0) {
+            for (int j = 0; j < 16; j++)
+              if ((j >> regpos[lb]) & 1) rpart |= (uint64_t)1 << (4 * j + sh);
+          } else if (lb >= 0) {
+            f.tb[i] = (int8_t)lb;
+            nonreg_bits |= 1u << sh;
+          } else {
+            f.ob[i] = (int8_t)h.tpos[i];
+            nonreg_bits |= 1u << sh;
+          }
+        }
+        f.rpart = rpart;
+        if (h.sign_only) {
+          f.type = FOP_SIGN;
+          for (int tp = 0; tp < 8; tp++) {
+            if (tp & ~nonreg_bits) continue;
+            unsigned nm = 0;
+            for (int j = 0; j < 16; j++) {
+              const int idx = (int)((rpart >> (4 * j)) & 15) | tp;
+              if (((jm >> j) & 1) && ((h.sign_mask >> idx) & 1)) nm |= 1u << j;
+            }
+            f.neg[tp] = (uint16_t)nm;
+          }
+        } else {
+          f.type = FOP_DIAG;
+          f.coef = (uint32_t)ncoef;
+          for (int i = 0; i < (1 << h.nt); i++) pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+        }
+      }
+    }
+    // merge runs of uncontrolled one-target dense ops into FOP_D1RUN records
+    {
+      int w = P.op_begin;
+      for (int r = P.op_begin; r < nops;) {
+        FOp f = pp->ops[r];
+        const bool plain1 = f.type == FOP_DENSE1 && f.omask == 0 && f.tmask == 0 && f.jmask == 0xffffu;
+        if (!plain1) {
+          pp->ops[w++] = f;
+          r++;
+          continue;
+        }
+        FOp run;
+        memset(&run, 0, sizeof(run));
+        run.type = FOP_D1RUN;
+        run.coef = f.coef;
+        int k = 0;
+        // coefficients of consecutive dense1 ops are contiguous (4 each, in emission order)
+        while (r < nops && k < 4) {
+          const FOp& g2 = pp->ops[r];
+          const bool ok = g2.type == FOP_DENSE1 && g2.omask == 0 && g2.tmask == 0 && g2.jmask == 0xffffu &&
+                          g2.coef == run.coef + 4u * (unsigned)k;
+          if (!ok) break;
+          run.ru[k++] = g2.u0;
+          r++;
+        }
+        run.nrun = (uint8_t)k;
+        pp->ops[w++] = run;
+      }
+      nops = w;
+    }
+    for (int q = P.op_begin; q < nops; q++) {
+      FOp& f = pp->ops[q];
+      f.flags = (uint8_t)((f.omask ? FLAG_OMASK : 0) | (f.tmask ? FLAG_TMASK : 0));
+    }
+    P.op_end = (uint16_t)nops;
+  }
+  pp->nphases = (int)groups.size();
+  pp->nops = nops;
+  *nphases_out = (int)groups.size();
+}
+
+template <typename T>
+static int build_program(sv_program* prog) {
+  const int n = prog->nqubits;
+  const int kt = prog->kt;
+  const int coef_cap = kCoefBytes / (int)sizeof(T);
+  prog->pass_bytes = sizeof(PassParams<T>);
+  // split at unfusable ops (dense on more than 2 targets, diagonal on more than 3)
+  std::vector<std::vector<int>> runs(1);
+  std::vector<int> barriers;
+  for (size_t i = 0; i < prog->ops.size(); i++) {
+    const HostOp& h = prog->ops[i];
+    const bool fusable = (h.kind == SV_OP_DIAG && h.nt <= 3) || (h.kind == SV_OP_DENSE && h.nt <= 2);
+    if (fusable) {
+      runs.back().push_back((int)i);
+    } else {
+      barriers.push_back((int)i);
+      runs.emplace_back();
+    }
+  }
+  for (size_t r = 0; r < runs.size(); r++) {
+    std::vector<int> rem = runs[r];
+    while (!rem.empty()) {
+      // greedy in gate order: a gate joins while its dense targets fit in the tile
+      // and none of its qubits is held back by an earlier gate left for later
+      uint64_t S = (1ull << kLowBits) - 1;
+      int ssize = kLowBits;
+      uint64_t blocked = 0;
+      int nops = 0, ncoef = 0;
+      bool full = false;
+      std::vector<int> sched, next;
+      for (int oi : rem) {
+        const HostOp& h = prog->ops[oi];
+        uint64_t tbits = 0, bits = 0;
+        for (int i = 0; i < h.nt; i++) tbits |= 1ull << h.tpos[i];
+        bits = tbits;
+        for (int i = 0; i < h.nc; i++) bits |= 1ull << h.cpos[i];
+        const int cc = coef_cost(h);
+        if (full || (bits & blocked) || nops + 1 > kMaxPassOps || ncoef + cc > coef_cap) {
+          if (nops + 1 > kMaxPassOps || ncoef + cc > coef_cap) full = true;
+          blocked |= bits;
+          next.push_back(oi);
+          continue;
+        }
+        if (h.kind == SV_OP_DENSE) {
+          const uint64_t need = tbits & ~S;
+          const int nneed = __builtin_popcountll(need);
+          if (ssize + nneed > kt) {
+            blocked |= bits;
+            next.push_back(oi);
+            continue;
+          }
+          S |= need;
+          ssize += nneed;
+        }
+        sched.push_back(oi);
+        nops++;
+        ncoef += cc;
+      }
+      for (int b = 0; b < n && ssize < kt; b++)
+        if (!((S >> b) & 1)) {
+          S |= 1ull << b;
+          ssize++;
+        }
+      const size_t off = prog->passes.size();
+      prog->passes.resize(off + sizeof(PassParams<T>));
+      int nph = 0;
+      encode_pass<T>(prog, sched, S, reinterpret_cast<PassParams<T>*>(prog->passes.data() + off), &nph);
+      Segment seg;
+      seg.fused = true;
+      seg.pass = prog->npasses;
+      prog->segments.push_back(seg);
+      prog->npasses++;
+      prog->nphases += nph;
+      prog->nfused_gates += (int)sched.size();
+      rem.swap(next);
+    }
+    if (r < barriers.size()) {
+      Segment seg;
+      seg.host_op = barriers[r];
+      prog->segments.push_back(seg);
+      prog->nunfused++;
+    }
+  }
+  return SV_OK;
+}
+
+template <typename T>
+static size_t pass_smem(int kt) {
+  const int tsize = 1 << kt;
+  return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
+}
+
+template <typename T>
+static int run_program(Context* ctx, const sv_program* prog, void* state) {
+  const int n = prog->nqubits, kt = prog->kt;
+  const size_t smem = pass_smem<T>(kt);
+  // the attribute is one value per kernel: raise it to the largest tile ever run
+  static size_t attr_bytes = 0;
+  if (smem > attr_bytes) {
+    SV_TRY(check_cuda(cudaFuncSetAttribute(k_fused_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "fused pass smem attribute"));
+    attr_bytes = smem;
+  }
+  const int threads = 1 << (kt - kRB);
+  if (threads > fused_max_threads<T>())
+    return set_error(SV_ERR_ARG, "tile_bits %d too large for this dtype (at most %d)", kt,
+                     kRB + (sizeof(T) >= 16 ? 8 : 9));
+  int per_sm = 0;
+  SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_pass<T>, threads, smem),
+                    "fused pass occupancy"));
+  if (per_sm < 1) return set_error(SV_ERR_ARG, "tile of 2^%d amplitudes does not fit on an SM", kt);
+  const int64_t ntiles = (int64_t)1 << (n - kt);
+  for (const Segment& s : prog->segments) {
+    if (s.fused) {
+      const PassParams<T>& p =
+          *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
+      int64_t grid = (int64_t)per_sm * ctx->num_sms;
+      if (grid > ntiles) grid = ntiles;
+      k_fused_pass<T><<<(unsigned)grid, threads, smem, ctx->stream>>>((T*)state, p);
+      SV_LAUNCH_CHECK("fused pass launch");
+    } else {
+      const HostOp& h = prog->ops[s.host_op];
+      std::vector<int32_t> targets(h.nt), qubits;
+      for (int i = 0; i < h.nt; i++) {
+        targets[i] = n - 1 - h.tpos[i];
+        qubits.push_back(h.tpos[i]);
+      }
+      for (int i = 0; i < h.nc; i++) qubits.push_back(h.cpos[i]);
+      std::sort(qubits.begin(), qubits.end());
+      const size_t d = (size_t)1 << h.nt;
+      std::vector<T> dense(d * d);
+      if (h.kind == SV_OP_DIAG) {  // a diagonal on more than 3 bits: apply as a dense matrix
+        const double zero[2] = {0.0, 0.0};
+        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<T>(zero);
+        for (size_t i = 0; i < d; i++) dense[i * d + i] = to_elem<T>(&h.m[2 * i]);
+      } else {
+        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<T>(&h.m[2 * i]);
+      }
+      SV_TRY(sv_apply_multi_qubit(static_cast<sv_context*>(ctx), state, prog->dtype, n, dense.data(), targets.data(),
+                                  h.nt, qubits.data(), (int)qubits.size()));
+    }
+  }
+  return SV_OK;
+}
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" {
+
+int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op* ops, int nops, int tile_bits,
+                      sv_program** out) {
+  if (!ctx || !out) return set_error(SV_ERR_ARG, "null context or output");
+  *out = nullptr;
+  if (dtype != SV_C128 && dtype != SV_C64) return set_error(SV_ERR_UNSUPPORTED, "fused programs need a complex dtype");
+  if (nqubits < kLowBits + kRB || nqubits > kMaxQubits)
+    return set_error(SV_ERR_ARG, "fused programs need %d..%d qubits", kLowBits + kRB, kMaxQubits);
+  if (nops < 0 || (nops > 0 && !ops)) return set_error(SV_ERR_ARG, "bad op list");
+  int kt = tile_bits;
+  if (kt <= 0) kt = dtype == SV_C128 ? 11 : 12;
+  if (kt > nqubits) kt = nqubits;
+  const int kt_max = kRB + (dtype == SV_C128 ? 8 : 9);
+  if (kt < kLowBits + kRB || kt > kt_max)
+    return set_error(SV_ERR_ARG, "tile_bits must be in [%d, %d]", kLowBits + kRB, kt_max);
+  sv_program* prog = new sv_program();
+  prog->dtype = dtype;
+  prog->nqubits = nqubits;
+  prog->kt = kt;
+  for (int i = 0; i < nops; i++) {
+    const sv_gate_op& g = ops[i];
+    HostOp h;
+    h.kind = g.kind;
+    h.nt = g.ntargets;
+    h.nc = g.ncontrols;
+    const bool ok_kind = g.kind == SV_OP_DENSE || g.kind == SV_OP_DIAG;
+    if (!ok_kind || g.ntargets < 1 || g.ntargets > kMaxTargets || g.ncontrols < 0 || g.ncontrols > 16 ||
+        !g.matrix) {
+      delete prog;
+      return set_error(SV_ERR_ARG, "op %d: bad kind, target count, control count or matrix", i);
+    }
+    uint64_t seen = 0;
+    for (int k = 0; k < g.ntargets + g.ncontrols; k++) {
+      const int q = k < g.ntargets ? g.targets[k] : g.controls[k - g.ntargets];
+      if (q < 0 || q >= nqubits || ((seen >> q) & 1)) {
+        delete prog;
+        return set_error(SV_ERR_ARG, "op %d: qubit %d out of range or repeated", i, q);
+      }
+      seen |= 1ull << q;
+      if (k < g.ntargets) h.tpos[k] = nqubits - 1 - q;
+      else h.cpos[k - g.ntargets] = nqubits - 1 - q;
+    }
+    const size_t ne = g.kind == SV_OP_DENSE ? ((size_t)1 << (2 * g.ntargets)) : ((size_t)1 << g.ntargets);
+    h.m.assign(g.matrix, g.matrix + 2 * ne);
+    if (g.kind == SV_OP_DIAG) {
+      h.sign_only = true;
+      for (size_t e = 0; e < ne; e++) {
+        const double re = h.m[2 * e], im = h.m[2 * e + 1];
+        if (im != 0.0 || (re != 1.0 && re != -1.0)) h.sign_only = false;
+        if (re == -1.0 && im == 0.0) h.sign_mask |= 1 << e;
+      }
+    }
+    prog->ops.push_back(std::move(h));
+  }
+  const int rc = dtype == SV_C128 ? build_program<c128>(prog) : build_program<c64>(prog);
+  if (rc != SV_OK) {
+    delete prog;
+    return rc;
+  }
+  *out = prog;
+  return SV_OK;
+}
+
+int sv_program_run(sv_context* ctx, const sv_program* prog, void* state) {
+  if (!ctx || !prog || !state) return set_error(SV_ERR_ARG, "null context, program or state");
+  if (((uintptr_t)state) % 16) return set_error(SV_ERR_ARG, "state must be 16-byte aligned");
+  return prog->dtype == SV_C128 ? run_program<c128>(ctx, prog, state) : run_program<c64>(ctx, prog, state);
+}
+
+int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* nfused_gates, int* tile_bits) {
+  if (!prog) return set_error(SV_ERR_ARG, "null program");
+  if (npasses) *npasses = prog->npasses;
+  if (nunfused) *nunfused = prog->nunfused;
+  if (nfused_gates) *nfused_gates = prog->nfused_gates;
+  if (tile_bits) *tile_bits = prog->kt;
+  return SV_OK;
+}
+
+int sv_program_destroy(sv_program* prog) {
+  delete prog;
+  return SV_OK;
+}
+
+}  // extern "C"

@@ -743,3 +743,186 @@ extern "C" int sv_collapse_state_noalloc(void* stream, void* state, int dtype, i
     default: return collapse_noalloc_typed<float>(s, *d, state, nqubits, m, normalize);
   }
 }
+
+// ===================================================================== reductions
+// FP64 reductions over states of either precision (the precision mode keeps bulk
+// arithmetic in complex64 and every reduction in FP64): <a|b>, max |a_i - b_i|, and
+// <Z_mask> = sum_i (-1)^popcount(i & mask) |a_i|^2.  Per-thread Neumaier sums, fixed
+// grid, fixed-order final sums: results are reproducible run to run.
+namespace sv {
+
+template <typename T>
+__device__ __forceinline__ void as_f64(T a, double& re, double& im) {
+  if constexpr (is_complex<T>::value) {
+    re = (double)a.re;
+    im = (double)a.im;
+  } else {
+    re = (double)a;
+    im = 0.0;
+  }
+}
+
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(kOpsBlock) k_dot_partials(const TA* __restrict__ a, const TB* __restrict__ b,
+                                                           int64_t n, double* __restrict__ partials) {
+  KSum sre, sim;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double ar, ai, br, bi;
+    as_f64(ldg_stream(a + i), ar, ai);
+    as_f64(ldg_stream(b + i), br, bi);
+    sre.add(ar * br + ai * bi);  // conj(a) * b
+    sim.add(ar * bi - ai * br);
+  }
+  const double r = block_sum(sre.value());
+  const double m = block_sum(sim.value());
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = r;
+    partials[2 * blockIdx.x + 1] = m;
+  }
+}
+
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(kOpsBlock) k_maxdiff_partials(const TA* __restrict__ a, const TB* __restrict__ b,
+                                                               int64_t n, double* __restrict__ partials) {
+  double mx = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double ar, ai, br, bi;
+    as_f64(ldg_stream(a + i), ar, ai);
+    as_f64(ldg_stream(b + i), br, bi);
+    mx = fmax(mx, hypot(ar - br, ai - bi));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  __shared__ double part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = fmax(r, part[w]);
+    partials[blockIdx.x] = r;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOpsBlock) k_zexp_partials(const T* __restrict__ s, int64_t n, int64_t mask,
+                                                            double* __restrict__ partials) {
+  KSum acc;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double p = tnorm2(ldg_stream(s + i));
+    acc.add((__popcll((unsigned long long)(i & mask)) & 1) ? -p : p);
+  }
+  const double r = block_sum(acc.value());
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+}
+
+// host: fixed-order compensated sum of the partials
+static double host_ksum(const double* v, int n, int stride) {
+  double s = 0.0, c = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double x = v[(size_t)i * stride];
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  return s + c;
+}
+
+template <typename TA, typename TB>
+static int dot_typed(Context* ctx, const void* a, const void* b, int64_t n, double* out, bool maxdiff) {
+  const unsigned grid = stream_grid(ctx, n);
+  const size_t bytes = sizeof(double) * 2 * grid;
+  SV_TRY(ensure_scratch(ctx, bytes));
+  SV_TRY(ensure_host_pinned(ctx, bytes));
+  double* d = (double*)ctx->scratch;
+  if (maxdiff) k_maxdiff_partials<TA, TB><<<grid, kOpsBlock, 0, ctx->stream>>>((const TA*)a, (const TB*)b, n, d);
+  else k_dot_partials<TA, TB><<<grid, kOpsBlock, 0, ctx->stream>>>((const TA*)a, (const TB*)b, n, d);
+  SV_LAUNCH_CHECK("reduction launch");
+  SV_TRY(check_cuda(cudaMemcpyAsync(ctx->host_pinned, d, bytes, cudaMemcpyDeviceToHost, ctx->stream), "reduction copy"));
+  SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "reduction sync"));
+  const double* h = (const double*)ctx->host_pinned;
+  if (maxdiff) {
+    double m = 0.0;
+    for (unsigned i = 0; i < grid; i++) m = fmax(m, h[i]);
+    out[0] = m;
+  } else {
+    out[0] = host_ksum(h, (int)grid, 2);
+    out[1] = host_ksum(h + 1, (int)grid, 2);
+  }
+  return SV_OK;
+}
+
+template <typename TA>
+static int dot_dispatch_b(Context* ctx, const void* a, const void* b, int dtb, int64_t n, double* out, bool maxdiff) {
+  switch (dtb) {
+    case SV_C128: return dot_typed<TA, c128>(ctx, a, b, n, out, maxdiff);
+    case SV_C64: return dot_typed<TA, c64>(ctx, a, b, n, out, maxdiff);
+    case SV_F64: return dot_typed<TA, double>(ctx, a, b, n, out, maxdiff);
+    default: return dot_typed<TA, float>(ctx, a, b, n, out, maxdiff);
+  }
+}
+
+static int dot_dispatch(Context* ctx, const void* a, int dta, const void* b, int dtb, int nqubits, double* out,
+                        bool maxdiff) {
+  SV_TRY(check_state(a, dta, nqubits));
+  SV_TRY(check_state(b, dtb, nqubits));
+  if (!out) return set_error(SV_ERR_ARG, "output pointer is NULL");
+  const int64_t n = (int64_t)1 << nqubits;
+  switch (dta) {
+    case SV_C128: return dot_dispatch_b<c128>(ctx, a, b, dtb, n, out, maxdiff);
+    case SV_C64: return dot_dispatch_b<c64>(ctx, a, b, dtb, n, out, maxdiff);
+    case SV_F64: return dot_dispatch_b<double>(ctx, a, b, dtb, n, out, maxdiff);
+    default: return dot_dispatch_b<float>(ctx, a, b, dtb, n, out, maxdiff);
+  }
+}
+
+template <typename T>
+static int zexp_typed(Context* ctx, const void* s, int64_t n, int64_t mask, double* out) {
+  const unsigned grid = stream_grid(ctx, n);
+  const size_t bytes = sizeof(double) * grid;
+  SV_TRY(ensure_scratch(ctx, bytes));
+  SV_TRY(ensure_host_pinned(ctx, bytes));
+  double* d = (double*)ctx->scratch;
+  k_zexp_partials<T><<<grid, kOpsBlock, 0, ctx->stream>>>((const T*)s, n, mask, d);
+  SV_LAUNCH_CHECK("expectation launch");
+  SV_TRY(check_cuda(cudaMemcpyAsync(ctx->host_pinned, d, bytes, cudaMemcpyDeviceToHost, ctx->stream), "expectation copy"));
+  SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "expectation sync"));
+  out[0] = host_ksum((const double*)ctx->host_pinned, (int)grid, 1);
+  return SV_OK;
+}
+
+}  // namespace sv
+
+extern "C" int sv_inner_product(sv_context* ctx, const void* a, int dtype_a, const void* b, int dtype_b, int nqubits,
+                                double* out_re_im) {
+  if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
+  return sv::dot_dispatch(ctx, a, dtype_a, b, dtype_b, nqubits, out_re_im, false);
+}
+
+extern "C" int sv_max_abs_diff(sv_context* ctx, const void* a, int dtype_a, const void* b, int dtype_b, int nqubits,
+                               double* out) {
+  if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
+  return sv::dot_dispatch(ctx, a, dtype_a, b, dtype_b, nqubits, out, true);
+}
+
+extern "C" int sv_expectation_z(sv_context* ctx, const void* state, int dtype, int nqubits, const int32_t* qubits,
+                                int nq, double* out) {
+  using namespace sv;
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  SV_TRY(check_state(state, dtype, nqubits));
+  if (!out || (nq > 0 && !qubits) || nq < 0) return set_error(SV_ERR_ARG, "bad qubit list or output");
+  int64_t mask = 0;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits) return set_error(SV_ERR_ARG, "qubit %d out of range", qubits[j]);
+    mask ^= (int64_t)1 << (nqubits - 1 - qubits[j]);
+  }
+  const int64_t n = (int64_t)1 << nqubits;
+  switch (dtype) {
+    case SV_C128: return zexp_typed<c128>(ctx, state, n, mask, out);
+    case SV_C64: return zexp_typed<c64>(ctx, state, n, mask, out);
+    case SV_F64: return zexp_typed<double>(ctx, state, n, mask, out);
+    default: return zexp_typed<float>(ctx, state, n, mask, out);
+  }
+}
