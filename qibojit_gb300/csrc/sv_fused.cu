@@ -178,9 +178,13 @@ __device__ __forceinline__ int64_t tile_origin(int64_t t, const int32_t* pos, in
 }
 
 // ------------------------------------------------------------------ tile kernel
-template <typename T>
-__global__ void __launch_bounds__(fused_max_threads<T>(), 1) k_fused_pass(T* __restrict__ state,
-                                                                      const __grid_constant__ PassParams<T> p) {
+// MAXT/MINB: threads per CTA and CTAs per SM the register allocation is sized for.
+// complex64 tiles of up to 2^12 amplitudes run three 256-thread CTAs per SM (80
+// registers); larger complex64 tiles and complex128 tiles (FP64-bound) run with the
+// whole register file.
+template <typename T, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state,
+                                                         const __grid_constant__ PassParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int kt = p.kt;
   const int tsize = 1 << kt;
@@ -240,8 +244,16 @@ __global__ void __launch_bounds__(fused_max_threads<T>(), 1) k_fused_pass(T* __r
           }
           const int nr = op.nrun;
           const T* c = p.coef + op.coef;
+          if (nr == 4) {
+            // the planner sorts a run of four gates on distinct bits into register order
+            dense1_regs<T, 0>(v, c, 0xffffu);
+            dense1_regs<T, 1>(v, c + 4, 0xffffu);
+            dense1_regs<T, 2>(v, c + 8, 0xffffu);
+            dense1_regs<T, 3>(v, c + 12, 0xffffu);
+          } else {
 #pragma unroll 1
-          for (int k = 0; k < nr; k++) dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+            for (int k = 0; k < nr; k++) dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+          }
           continue;
         }
         const int flags = op.flags;
@@ -492,16 +504,27 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         run.type = FOP_D1RUN;
         run.coef = f.coef;
         int k = 0;
-        // coefficients of consecutive dense1 ops are contiguous (4 each, in emission order)
+        unsigned used = 0;
+        // coefficients of consecutive dense1 ops are contiguous (4 each, in emission order);
+        // a run holds gates on distinct register bits, which commute
         while (r < nops && k < 4) {
           const FOp& g2 = pp->ops[r];
           const bool ok = g2.type == FOP_DENSE1 && g2.omask == 0 && g2.tmask == 0 && g2.jmask == 0xffffu &&
-                          g2.coef == run.coef + 4u * (unsigned)k;
+                          g2.coef == run.coef + 4u * (unsigned)k && !((used >> g2.u0) & 1u);
           if (!ok) break;
+          used |= 1u << g2.u0;
           run.ru[k++] = g2.u0;
           r++;
         }
         run.nrun = (uint8_t)k;
+        if (k == 4) {
+          // reorder the four (commuting) gates and their matrices into register order 0..3
+          T tmp[16];
+          for (int q = 0; q < 4; q++)
+            for (int e = 0; e < 4; e++) tmp[4 * run.ru[q] + e] = pp->coef[run.coef + 4 * q + e];
+          for (int e = 0; e < 16; e++) pp->coef[run.coef + e] = tmp[e];
+          for (int q = 0; q < 4; q++) run.ru[q] = (uint8_t)q;
+        }
         pp->ops[w++] = run;
       }
       nops = w;
@@ -609,34 +632,55 @@ static size_t pass_smem(int kt) {
   return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
 }
 
+template <typename T, int MAXT, int MINB>
+static int launch_variant(Context* ctx, const PassParams<T>& p, void* state, int threads, size_t smem,
+                          int64_t ntiles) {
+  auto kern = k_fused_pass<T, MAXT, MINB>;
+  // the attribute is one value per kernel: raise it to the largest tile ever run
+  static size_t attr_bytes = 0;
+  if (smem > attr_bytes) {
+    SV_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "fused pass smem attribute"));
+    attr_bytes = smem;
+  }
+  static int per_sm_cache[kMaxTile + 1] = {0};
+  int& per_sm = per_sm_cache[p.kt];
+  if (per_sm == 0) {
+    SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
+                      "fused pass occupancy"));
+    if (per_sm < 1) return set_error(SV_ERR_ARG, "tile of 2^%d amplitudes does not fit on an SM", p.kt);
+  }
+  int64_t grid = (int64_t)per_sm * ctx->num_sms;
+  if (grid > ntiles) grid = ntiles;
+  kern<<<(unsigned)grid, threads, smem, ctx->stream>>>((T*)state, p);
+  SV_LAUNCH_CHECK("fused pass launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int launch_pass(Context* ctx, const PassParams<T>& p, void* state, int threads, size_t smem, int64_t ntiles) {
+  if constexpr (sizeof(T) >= 16) {
+    return launch_variant<T, 256, 1>(ctx, p, state, threads, smem, ntiles);
+  } else {
+    if (threads <= 256) return launch_variant<T, 256, 3>(ctx, p, state, threads, smem, ntiles);
+    return launch_variant<T, 512, 1>(ctx, p, state, threads, smem, ntiles);
+  }
+}
+
 template <typename T>
 static int run_program(Context* ctx, const sv_program* prog, void* state) {
   const int n = prog->nqubits, kt = prog->kt;
   const size_t smem = pass_smem<T>(kt);
-  // the attribute is one value per kernel: raise it to the largest tile ever run
-  static size_t attr_bytes = 0;
-  if (smem > attr_bytes) {
-    SV_TRY(check_cuda(cudaFuncSetAttribute(k_fused_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "fused pass smem attribute"));
-    attr_bytes = smem;
-  }
   const int threads = 1 << (kt - kRB);
   if (threads > fused_max_threads<T>())
     return set_error(SV_ERR_ARG, "tile_bits %d too large for this dtype (at most %d)", kt,
                      kRB + (sizeof(T) >= 16 ? 8 : 9));
-  int per_sm = 0;
-  SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_pass<T>, threads, smem),
-                    "fused pass occupancy"));
-  if (per_sm < 1) return set_error(SV_ERR_ARG, "tile of 2^%d amplitudes does not fit on an SM", kt);
   const int64_t ntiles = (int64_t)1 << (n - kt);
   for (const Segment& s : prog->segments) {
     if (s.fused) {
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
-      int64_t grid = (int64_t)per_sm * ctx->num_sms;
-      if (grid > ntiles) grid = ntiles;
-      k_fused_pass<T><<<(unsigned)grid, threads, smem, ctx->stream>>>((T*)state, p);
-      SV_LAUNCH_CHECK("fused pass launch");
+      SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles));
     } else {
       const HostOp& h = prog->ops[s.host_op];
       std::vector<int32_t> targets(h.nt), qubits;
