@@ -206,6 +206,26 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
                      int* tile_bits);
 int sv_program_destroy(sv_program* prog);
 
+/* ---------------------------------------------------------- batched circuits */
+/* Many circuits of uneven size (8..34 qubits) in one job, for variational workloads
+ * (the reference runs circuits one at a time through execute_circuit).  Circuits with
+ * the same gate structure share one plan; each run zeroes every state and applies
+ * every circuit as batched fused-pass launches spread over several streams; the
+ * first run also records them as a CUDA graph that later runs replay.  States live
+ * in one device buffer owned by the batch. */
+typedef struct sv_batch sv_batch;
+int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubits, const sv_gate_op* const* ops,
+                    const int32_t* nops, int tile_bits, sv_batch** out);
+/* |0...0> then every circuit; asynchronous on the context stream. */
+int sv_batch_run(sv_context* ctx, sv_batch* b);
+/* Transverse-field Ising energies E_c = -sum_i <Z_i Z_{i+1}> - h sum_i <X_i> (open chain),
+ * FP64 accumulation; `energies` (host) receives ncirc values; synchronises. */
+int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energies);
+/* Device pointer and qubit count of one circuit's state. */
+int sv_batch_state(const sv_batch* b, int circuit, void** state, int* nqubits);
+int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_bytes);
+int sv_batch_destroy(sv_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

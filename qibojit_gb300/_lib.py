@@ -29,6 +29,8 @@ EXPORTS = (
     "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_measure_frequencies",
     "sv_collapse_state_noalloc", "sv_program_create", "sv_program_run", "sv_program_stats",
     "sv_program_destroy", "sv_inner_product", "sv_max_abs_diff", "sv_expectation_z",
+    "sv_batch_create", "sv_batch_run", "sv_batch_tfim_energy", "sv_batch_state", "sv_batch_stats",
+    "sv_batch_destroy",
 )
 
 
@@ -67,6 +69,12 @@ _SIGNATURES = {
     "sv_inner_product": ([_vp, _vp, _int, _vp, _int, _int, _vp], _int),
     "sv_max_abs_diff": ([_vp, _vp, _int, _vp, _int, _int, _vp], _int),
     "sv_expectation_z": ([_vp, _vp, _int, _int, _vp, _int, _vp], _int),
+    "sv_batch_create": ([_vp, _int, _int, _vp, _vp, _vp, _int, ctypes.POINTER(_vp)], _int),
+    "sv_batch_run": ([_vp, _vp], _int),
+    "sv_batch_tfim_energy": ([_vp, _vp, ctypes.c_double, _vp], _int),
+    "sv_batch_state": ([_vp, _int, ctypes.POINTER(_vp), ctypes.POINTER(_int)], _int),
+    "sv_batch_stats": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_size_t)], _int),
+    "sv_batch_destroy": ([_vp], _int),
 }
 
 

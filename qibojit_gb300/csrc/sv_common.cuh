@@ -160,9 +160,9 @@ int ensure_scratch(Context* ctx, size_t bytes);
 int ensure_host_pinned(Context* ctx, size_t bytes);
 int ensure_operand(Context* ctx, size_t bytes);
 
-#define SV_TRY(expr)                 \
+#define SV_TRY(...)                  \
   do {                               \
-    int _rc = (expr);                \
+    int _rc = (__VA_ARGS__);         \
     if (_rc != SV_OK) return _rc;    \
   } while (0)
 

@@ -35,7 +35,16 @@ constexpr int kLowBits = 4;       // lowest bits always in a tile (contiguous ru
 constexpr int kMaxPassOps = 128;  // ops (and phases) per pass
 constexpr int kCoefBytes = 12288; // coefficient bytes per pass
 
-enum : uint8_t { FOP_DENSE1 = 0, FOP_DENSE2 = 1, FOP_DIAG = 2, FOP_SIGN = 3, FOP_D1RUN = 4 };
+enum : uint8_t {
+  FOP_DENSE1 = 0,   // complex 2x2
+  FOP_DENSE2 = 1,   // complex 4x4
+  FOP_DIAG = 2,     // diagonal phases on up to 3 bits
+  FOP_SIGN = 3,     // diagonal with entries +-1 (CZ, Z, CCZ): folded into a negate mask
+  FOP_D1RUN = 4,    // up to 4 uncontrolled complex 2x2 on distinct register bits
+  FOP_X1 = 5,       // X (CNOT, Toffoli targets): a register swap, no arithmetic
+  FOP_DENSE1R = 6,  // real 2x2 (RY, H): half the flops of a complex one
+  FOP_SWAP2 = 7     // SWAP: exchange of |01> and |10>, no arithmetic
+};
 enum : uint8_t { FLAG_OMASK = 1, FLAG_TMASK = 2 };
 
 // One op in phase-local form (64 bytes).
@@ -69,7 +78,7 @@ struct PassParams {
   int32_t n, kt, nphases, nops;
   int64_t ntiles;
   int32_t tile_pos[kMaxTile];  // global bit positions of the tile bits, ascending
-  int32_t pad;
+  int32_t coef_goff;           // batched runs: this pass's first coefficient in a circuit's block
   Phase phases[kMaxPassOps];
   FOp ops[kMaxPassOps];
   T coef[kCoefBytes / sizeof(T)];
@@ -148,6 +157,78 @@ __device__ __forceinline__ void dense1_dispatch(T (&v)[16], const T* m, int u, u
   }
 }
 
+template <typename T, int U>
+__device__ __forceinline__ void x1_regs(T (&v)[16], unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const T t = v[j];
+    v[j] = v[j | (1 << U)];
+    v[j | (1 << U)] = t;
+  }
+}
+
+// real 2x2 on complex amplitudes: coefficients' imaginary parts are zero
+template <typename T, int U>
+__device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+  if constexpr (is_complex<T>::value) {
+    const auto a = m[0].re, b = m[1].re, c = m[2].re, d = m[3].re;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      if (j & (1 << U)) continue;
+      if (!((jm >> j) & 1u)) continue;
+      const int k = j | (1 << U);
+      const T x = v[j], y = v[k];
+      v[j].re = fma(a, x.re, b * y.re);
+      v[j].im = fma(a, x.im, b * y.im);
+      v[k].re = fma(c, x.re, d * y.re);
+      v[k].im = fma(c, x.im, d * y.im);
+    }
+  }
+}
+
+template <typename T, int U0, int U1>
+__device__ __forceinline__ void swap2_regs(T (&v)[16], unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & ((1 << U0) | (1 << U1))) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const T t = v[j | (1 << U1)];
+    v[j | (1 << U1)] = v[j | (1 << U0)];
+    v[j | (1 << U0)] = t;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void x1_dispatch(T (&v)[16], int u, unsigned jm) {
+  switch (u) {
+    case 0: x1_regs<T, 0>(v, jm); break;
+    case 1: x1_regs<T, 1>(v, jm); break;
+    case 2: x1_regs<T, 2>(v, jm); break;
+    default: x1_regs<T, 3>(v, jm); break;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dense1r_dispatch(T (&v)[16], const T* m, int u, unsigned jm) {
+  switch (u) {
+    case 0: dense1r_regs<T, 0>(v, m, jm); break;
+    case 1: dense1r_regs<T, 1>(v, m, jm); break;
+    case 2: dense1r_regs<T, 2>(v, m, jm); break;
+    default: dense1r_regs<T, 3>(v, m, jm); break;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void swap2_dispatch(T (&v)[16], int u0, int u1, unsigned jm) {
+  const int a = u0 < u1 ? u0 : u1, b = u0 < u1 ? u1 : u0;  // symmetric in its two targets
+#define SV_S2(A, B) \
+  if (a == A && b == B) { swap2_regs<T, A, B>(v, jm); return; }
+  SV_S2(0, 1) SV_S2(0, 2) SV_S2(0, 3) SV_S2(1, 2) SV_S2(1, 3) SV_S2(2, 3)
+#undef SV_S2
+}
+
 template <typename T>
 __device__ __forceinline__ void apply_negations(T (&v)[16], unsigned nm) {
 #pragma unroll
@@ -182,9 +263,22 @@ __device__ __forceinline__ int64_t tile_origin(int64_t t, const int32_t* pos, in
 // complex64 tiles of up to 2^12 amplitudes run three 256-thread CTAs per SM (80
 // registers); larger complex64 tiles and complex128 tiles (FP64-bound) run with the
 // whole register file.
-template <typename T, int MAXT, int MINB>
+// Batched runs: many circuits with the same pass structure (same gates on the same
+// qubits, different parameters) share one launch; work item = (circuit, tile), each
+// circuit has its own state and its own coefficient block in global memory.
+template <typename T>
+struct BatchArgs {
+  T* const* states;        // device array of per-circuit state pointers
+  const T* coef;           // per-circuit coefficient blocks, coef_stride apart
+  int64_t coef_stride;
+  int32_t ncirc;
+  int32_t pad;
+};
+
+template <typename T, int MAXT, int MINB, bool BATCHED>
 __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state,
-                                                         const __grid_constant__ PassParams<T> p) {
+                                                         const __grid_constant__ PassParams<T> p,
+                                                         const __grid_constant__ BatchArgs<T> batch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int kt = p.kt;
   const int tsize = 1 << kt;
@@ -200,20 +294,32 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
   }
   __syncthreads();
   const int nthreads = blockDim.x;
-  auto issue_load = [&](T* buf, int64_t base) {
+  auto issue_load = [&](T* buf, const T* st, int64_t base) {
     for (int e = threadIdx.x; e < tsize; e += nthreads)
-      cp_async<sizeof(T)>(buf + smem_pos(e), state + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))));
+      cp_async<sizeof(T)>(buf + smem_pos(e), st + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))));
     cp_async_commit();
   };
+  // items: (circuit, tile) for batched runs, tiles of the one state otherwise
+  const int64_t nitems = BATCHED ? p.ntiles * batch.ncirc : p.ntiles;
+  const int tshift = p.n - kt;  // ntiles = 2^tshift
+  auto item_state = [&](int64_t it) -> T* {
+    if constexpr (BATCHED) return batch.states[it >> tshift];
+    else return state;
+  };
+  auto item_tile = [&](int64_t it) -> int64_t { return BATCHED ? (it & (p.ntiles - 1)) : it; };
   int64_t t = blockIdx.x;
-  if (t < p.ntiles) issue_load(buf0, tile_origin(t, p.tile_pos, kt));
+  if (t < nitems) issue_load(buf0, item_state(t), tile_origin(item_tile(t), p.tile_pos, kt));
   int cur = 0;
-  for (; t < p.ntiles; t += gridDim.x, cur ^= 1) {
+  for (; t < nitems; t += gridDim.x, cur ^= 1) {
     T* tile = buf0 + cur * tstride;
-    const int64_t base = tile_origin(t, p.tile_pos, kt);
+    T* const st = item_state(t);
+    const int64_t base = tile_origin(item_tile(t), p.tile_pos, kt);
+    const T* cbase;
+    if constexpr (BATCHED) cbase = batch.coef + (t >> tshift) * batch.coef_stride + p.coef_goff;
+    else cbase = p.coef;
     const int64_t tn = t + gridDim.x;
-    if (tn < p.ntiles) {
-      issue_load(buf0 + (cur ^ 1) * tstride, tile_origin(tn, p.tile_pos, kt));
+    if (tn < nitems) {
+      issue_load(buf0 + (cur ^ 1) * tstride, item_state(tn), tile_origin(item_tile(tn), p.tile_pos, kt));
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
@@ -243,7 +349,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
             pending_neg = 0;
           }
           const int nr = op.nrun;
-          const T* c = p.coef + op.coef;
+          const T* c = cbase + op.coef;
           if (nr == 4) {
             // the planner sorts a run of four gates on distinct bits into register order
             dense1_regs<T, 0>(v, c, 0xffffu);
@@ -259,18 +365,21 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
         const int flags = op.flags;
         if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
         if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;
-        if (type == FOP_DENSE1) {
+        if (type == FOP_DENSE1 || type == FOP_DENSE1R || type == FOP_X1 || type == FOP_SWAP2) {
           if (pending_neg) {
             apply_negations(v, pending_neg);
             pending_neg = 0;
           }
-          dense1_dispatch(v, p.coef + op.coef, op.u0, op.jmask);
+          if (type == FOP_DENSE1) dense1_dispatch(v, cbase + op.coef, op.u0, op.jmask);
+          else if (type == FOP_DENSE1R) dense1r_dispatch(v, cbase + op.coef, op.u0, op.jmask);
+          else if (type == FOP_X1) x1_dispatch(v, op.u0, op.jmask);
+          else swap2_dispatch(v, op.u0, op.u1, op.jmask);
         } else if (type == FOP_DENSE2) {
           if (pending_neg) {
             apply_negations(v, pending_neg);
             pending_neg = 0;
           }
-          dense2_dispatch(v, p.coef + op.coef, op.u0, op.u1, op.jmask);
+          dense2_dispatch(v, cbase + op.coef, op.u0, op.u1, op.jmask);
         } else {
           const int nd = op.nd;
           int tp = 0;
@@ -285,7 +394,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
           } else {
             const unsigned jm = op.jmask;
             const uint64_t rp = op.rpart;
-            const T* c = p.coef + op.coef;
+            const T* c = cbase + op.coef;
 #pragma unroll
             for (int j = 0; j < 16; j++) {
               if (!((jm >> j) & 1u)) continue;
@@ -301,7 +410,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
       __syncthreads();
     }
     for (int e = threadIdx.x; e < tsize; e += nthreads)
-      stg_stream(state + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))), tile[smem_pos(e)]);
+      stg_stream(st + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))), tile[smem_pos(e)]);
     __syncthreads();  // this buffer is refilled by the prefetch two tiles later
   }
 }
@@ -316,6 +425,9 @@ struct HostOp {
   std::vector<double> m;    // complex entries (re, im) pairs
   bool sign_only = false;   // diagonal with entries in {+1, -1}
   int sign_mask = 0;        // bit i set: entry i is -1
+  bool is_x = false;        // dense one-target [[0, 1], [1, 0]]
+  bool is_real = false;     // dense with all-real entries
+  bool is_swap = false;     // dense two-target SWAP
 };
 
 struct Segment {
@@ -332,6 +444,10 @@ struct sv_program {
   std::vector<sv::Segment> segments;
   std::vector<unsigned char> passes;  // PassParams<T> blocks, back to back
   size_t pass_bytes = 0;
+  // coefficient sources of all passes, back to back: (op index, entry) per slot
+  std::vector<int32_t> coef_src;
+  std::vector<size_t> pass_coef_off;
+  size_t coef_total = 0;
   int npasses = 0, nunfused = 0, nfused_gates = 0, nphases = 0;
 };
 
@@ -348,14 +464,19 @@ static T to_elem(const double* re_im) {
 }
 
 static int coef_cost(const HostOp& h) {
-  if (h.kind == SV_OP_DENSE) return h.nt == 1 ? 4 : 16;
+  if (h.kind == SV_OP_DENSE) {
+    if (h.is_x || (h.nt == 2 && h.is_swap)) return 0;
+    return h.nt == 1 ? 4 : 16;
+  }
   return h.sign_only ? 0 : (1 << h.nt);
 }
 
 // Builds the phase-local form of the scheduled ops of one pass.
+// Every coefficient slot of a pass records where it came from (op index, entry), so a
+// circuit with the same structure and other parameters can refill the slots.
 template <typename T>
 static void encode_pass(const sv_program* prog, const std::vector<int>& sched, uint64_t S, PassParams<T>* pp,
-                        int* nphases_out) {
+                        int* nphases_out, std::vector<int32_t>* src) {
   const int n = prog->nqubits, kt = prog->kt;
   memset(pp, 0, sizeof(*pp));
   pp->n = n;
@@ -430,7 +551,8 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
       unsigned jm = 0;
       unsigned tbits = 0;  // register bits that are targets of a dense op
       if (h.kind == SV_OP_DENSE) {
-        f.type = h.nt == 1 ? FOP_DENSE1 : FOP_DENSE2;
+        if (h.nt == 1) f.type = h.is_x ? FOP_X1 : (h.is_real ? FOP_DENSE1R : FOP_DENSE1);
+        else f.type = h.is_swap ? FOP_SWAP2 : FOP_DENSE2;
         f.u0 = (uint8_t)regpos[pd.lt[0]];
         tbits = 1u << f.u0;
         if (h.nt == 2) {
@@ -442,8 +564,12 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         if (reg_c == 0) jm = 0xffffu;  // no register-level controls: kernel skips the tests
         f.jmask = (uint16_t)jm;
         f.coef = (uint32_t)ncoef;
-        const int ne = h.nt == 1 ? 4 : 16;
-        for (int i = 0; i < ne; i++) pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+        const int ne = coef_cost(h);
+        for (int i = 0; i < ne; i++) {
+          src->push_back(pd.op);
+          src->push_back(i);
+          pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+        }
       } else {
         f.nd = (uint8_t)h.nt;
         for (int j = 0; j < 16; j++)
@@ -484,7 +610,11 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         } else {
           f.type = FOP_DIAG;
           f.coef = (uint32_t)ncoef;
-          for (int i = 0; i < (1 << h.nt); i++) pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+          for (int i = 0; i < (1 << h.nt); i++) {
+            src->push_back(pd.op);
+            src->push_back(i);
+            pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+          }
         }
       }
     }
@@ -520,9 +650,19 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         if (k == 4) {
           // reorder the four (commuting) gates and their matrices into register order 0..3
           T tmp[16];
+          int32_t tsrc[32];
           for (int q = 0; q < 4; q++)
-            for (int e = 0; e < 4; e++) tmp[4 * run.ru[q] + e] = pp->coef[run.coef + 4 * q + e];
-          for (int e = 0; e < 16; e++) pp->coef[run.coef + e] = tmp[e];
+            for (int e = 0; e < 4; e++) {
+              const int from = run.coef + 4 * q + e, to = 4 * run.ru[q] + e;
+              tmp[to] = pp->coef[from];
+              tsrc[2 * to] = (*src)[2 * from];
+              tsrc[2 * to + 1] = (*src)[2 * from + 1];
+            }
+          for (int e = 0; e < 16; e++) {
+            pp->coef[run.coef + e] = tmp[e];
+            (*src)[2 * (run.coef + e)] = tsrc[2 * e];
+            (*src)[2 * (run.coef + e) + 1] = tsrc[2 * e + 1];
+          }
           for (int q = 0; q < 4; q++) run.ru[q] = (uint8_t)q;
         }
         pp->ops[w++] = run;
@@ -606,7 +746,12 @@ static int build_program(sv_program* prog) {
       const size_t off = prog->passes.size();
       prog->passes.resize(off + sizeof(PassParams<T>));
       int nph = 0;
-      encode_pass<T>(prog, sched, S, reinterpret_cast<PassParams<T>*>(prog->passes.data() + off), &nph);
+      std::vector<int32_t> src;
+      encode_pass<T>(prog, sched, S, reinterpret_cast<PassParams<T>*>(prog->passes.data() + off), &nph, &src);
+      reinterpret_cast<PassParams<T>*>(prog->passes.data() + off)->coef_goff = (int32_t)prog->coef_total;
+      prog->pass_coef_off.push_back(prog->coef_total);
+      prog->coef_total += src.size() / 2;
+      prog->coef_src.insert(prog->coef_src.end(), src.begin(), src.end());
       Segment seg;
       seg.fused = true;
       seg.pass = prog->npasses;
@@ -632,10 +777,10 @@ static size_t pass_smem(int kt) {
   return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
 }
 
-template <typename T, int MAXT, int MINB>
-static int launch_variant(Context* ctx, const PassParams<T>& p, void* state, int threads, size_t smem,
-                          int64_t ntiles) {
-  auto kern = k_fused_pass<T, MAXT, MINB>;
+template <typename T, int MAXT, int MINB, bool BATCHED>
+static int launch_variant(Context* ctx, cudaStream_t stream, const PassParams<T>& p, void* state, int threads,
+                          size_t smem, int64_t nitems, const BatchArgs<T>& batch) {
+  auto kern = k_fused_pass<T, MAXT, MINB, BATCHED>;
   // the attribute is one value per kernel: raise it to the largest tile ever run
   static size_t attr_bytes = 0;
   if (smem > attr_bytes) {
@@ -651,19 +796,20 @@ static int launch_variant(Context* ctx, const PassParams<T>& p, void* state, int
     if (per_sm < 1) return set_error(SV_ERR_ARG, "tile of 2^%d amplitudes does not fit on an SM", p.kt);
   }
   int64_t grid = (int64_t)per_sm * ctx->num_sms;
-  if (grid > ntiles) grid = ntiles;
-  kern<<<(unsigned)grid, threads, smem, ctx->stream>>>((T*)state, p);
+  if (grid > nitems) grid = nitems;
+  kern<<<(unsigned)grid, threads, smem, stream>>>((T*)state, p, batch);
   SV_LAUNCH_CHECK("fused pass launch");
   return SV_OK;
 }
 
-template <typename T>
-static int launch_pass(Context* ctx, const PassParams<T>& p, void* state, int threads, size_t smem, int64_t ntiles) {
+template <typename T, bool BATCHED = false>
+static int launch_pass(Context* ctx, const PassParams<T>& p, void* state, int threads, size_t smem, int64_t nitems,
+                       cudaStream_t stream, const BatchArgs<T>& batch = BatchArgs<T>{}) {
   if constexpr (sizeof(T) >= 16) {
-    return launch_variant<T, 256, 1>(ctx, p, state, threads, smem, ntiles);
+    return launch_variant<T, 256, 1, BATCHED>(ctx, stream, p, state, threads, smem, nitems, batch);
   } else {
-    if (threads <= 256) return launch_variant<T, 256, 3>(ctx, p, state, threads, smem, ntiles);
-    return launch_variant<T, 512, 1>(ctx, p, state, threads, smem, ntiles);
+    if (threads <= 256) return launch_variant<T, 256, 3, BATCHED>(ctx, stream, p, state, threads, smem, nitems, batch);
+    return launch_variant<T, 512, 1, BATCHED>(ctx, stream, p, state, threads, smem, nitems, batch);
   }
 }
 
@@ -680,7 +826,7 @@ static int run_program(Context* ctx, const sv_program* prog, void* state) {
     if (s.fused) {
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
-      SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles));
+      SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles, ctx->stream));
     } else {
       const HostOp& h = prog->ops[s.host_op];
       std::vector<int32_t> targets(h.nt), qubits;
@@ -706,6 +852,148 @@ static int run_program(Context* ctx, const sv_program* prog, void* state) {
   return SV_OK;
 }
 
+static void classify(HostOp& h) {
+  const size_t ne = h.kind == SV_OP_DENSE ? ((size_t)1 << (2 * h.nt)) : ((size_t)1 << h.nt);
+  h.sign_only = false;
+  h.sign_mask = 0;
+  h.is_x = h.is_real = h.is_swap = false;
+  if (h.kind == SV_OP_DIAG) {
+    h.sign_only = true;
+    for (size_t e = 0; e < ne; e++) {
+      const double re = h.m[2 * e], im = h.m[2 * e + 1];
+      if (im != 0.0 || (re != 1.0 && re != -1.0)) h.sign_only = false;
+      if (re == -1.0 && im == 0.0) h.sign_mask |= 1 << e;
+    }
+    return;
+  }
+  h.is_real = true;
+  for (size_t e = 0; e < ne; e++)
+    if (h.m[2 * e + 1] != 0.0) h.is_real = false;
+  auto is = [&](const double* want, size_t n) {
+    for (size_t e = 0; e < n; e++)
+      if (h.m[2 * e] != want[e] || h.m[2 * e + 1] != 0.0) return false;
+    return true;
+  };
+  static const double X[4] = {0, 1, 1, 0};
+  static const double SW[16] = {1, 0, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 0, 0, 1};
+  if (h.nt == 1) h.is_x = is(X, 4);
+  if (h.nt == 2) h.is_swap = is(SW, 16);
+}
+
+// 2x2 of a one-target op (diagonal ops expanded), complex (re, im) pairs
+static void as_dense2x2(const HostOp& h, double out[8]) {
+  if (h.kind == SV_OP_DENSE) {
+    for (int i = 0; i < 8; i++) out[i] = h.m[i];
+  } else {
+    const double d[8] = {h.m[0], h.m[1], 0, 0, 0, 0, h.m[2], h.m[3]};
+    for (int i = 0; i < 8; i++) out[i] = d[i];
+  }
+}
+
+// Consecutive uncontrolled one-target gates on the same qubit (no other gate touching
+// that qubit in between) are multiplied into one 2x2: fewer ops, same result.
+static void merge_single_qubit(std::vector<HostOp>& ops, int nqubits) {
+  std::vector<HostOp> out;
+  std::vector<int> last(64, -1);  // index in `out` of the last op touching each bit
+  for (HostOp& h : ops) {
+    const bool single = h.nt == 1 && h.nc == 0;
+    const int t = h.tpos[0];
+    if (single && last[t] >= 0) {
+      HostOp& p = out[last[t]];
+      if (p.nt == 1 && p.nc == 0 && p.tpos[0] == t) {
+        if (p.kind == SV_OP_DIAG && h.kind == SV_OP_DIAG) {
+          for (int e = 0; e < 2; e++) {
+            const double ar = h.m[2 * e], ai = h.m[2 * e + 1], br = p.m[2 * e], bi = p.m[2 * e + 1];
+            p.m[2 * e] = ar * br - ai * bi;
+            p.m[2 * e + 1] = ar * bi + ai * br;
+          }
+        } else {
+          double A[8], B[8], C[8];
+          as_dense2x2(h, A);  // applied second
+          as_dense2x2(p, B);
+          for (int r = 0; r < 2; r++)
+            for (int c = 0; c < 2; c++) {
+              double re = 0, im = 0;
+              for (int k = 0; k < 2; k++) {
+                const double ar = A[2 * (2 * r + k)], ai = A[2 * (2 * r + k) + 1];
+                const double br = B[2 * (2 * k + c)], bi = B[2 * (2 * k + c) + 1];
+                re += ar * br - ai * bi;
+                im += ar * bi + ai * br;
+              }
+              C[2 * (2 * r + c)] = re;
+              C[2 * (2 * r + c) + 1] = im;
+            }
+          p.kind = SV_OP_DENSE;
+          p.m.assign(C, C + 8);
+        }
+        classify(p);
+        continue;
+      }
+    }
+    out.push_back(h);
+    const int idx = (int)out.size() - 1;
+    for (int i = 0; i < h.nt; i++) last[h.tpos[i]] = idx;
+    for (int i = 0; i < h.nc; i++) last[h.cpos[i]] = idx;
+  }
+  (void)nqubits;
+  ops.swap(out);
+}
+
+static int parse_ops(int nqubits, const sv_gate_op* ops, int nops, std::vector<HostOp>* out) {
+  out->clear();
+  for (int i = 0; i < nops; i++) {
+    const sv_gate_op& g = ops[i];
+    HostOp h;
+    h.kind = g.kind;
+    h.nt = g.ntargets;
+    h.nc = g.ncontrols;
+    const bool ok_kind = g.kind == SV_OP_DENSE || g.kind == SV_OP_DIAG;
+    if (!ok_kind || g.ntargets < 1 || g.ntargets > kMaxTargets || g.ncontrols < 0 || g.ncontrols > 16 || !g.matrix)
+      return set_error(SV_ERR_ARG, "op %d: bad kind, target count, control count or matrix", i);
+    uint64_t seen = 0;
+    for (int k = 0; k < g.ntargets + g.ncontrols; k++) {
+      const int q = k < g.ntargets ? g.targets[k] : g.controls[k - g.ntargets];
+      if (q < 0 || q >= nqubits || ((seen >> q) & 1))
+        return set_error(SV_ERR_ARG, "op %d: qubit %d out of range or repeated", i, q);
+      seen |= 1ull << q;
+      if (k < g.ntargets) h.tpos[k] = nqubits - 1 - q;
+      else h.cpos[k - g.ntargets] = nqubits - 1 - q;
+    }
+    const size_t ne = g.kind == SV_OP_DENSE ? ((size_t)1 << (2 * g.ntargets)) : ((size_t)1 << g.ntargets);
+    h.m.assign(g.matrix, g.matrix + 2 * ne);
+    classify(h);
+    out->push_back(std::move(h));
+  }
+  merge_single_qubit(*out, nqubits);
+  return SV_OK;
+}
+
+static int check_tile_bits(int dtype, int nqubits, int tile_bits, int* kt_out) {
+  int kt = tile_bits;
+  if (kt <= 0) kt = dtype == SV_C128 ? 11 : 12;
+  if (kt > nqubits) kt = nqubits;
+  const int kt_max = kRB + (dtype == SV_C128 ? 8 : 9);
+  if (kt < kLowBits + kRB || kt > kt_max)
+    return set_error(SV_ERR_ARG, "tile_bits must be in [%d, %d]", kLowBits + kRB, kt_max);
+  *kt_out = kt;
+  return SV_OK;
+}
+
+static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out) {
+  sv_program* prog = new sv_program();
+  prog->dtype = dtype;
+  prog->nqubits = nqubits;
+  prog->kt = kt;
+  prog->ops = std::move(ops);
+  const int rc = dtype == SV_C128 ? build_program<c128>(prog) : build_program<c64>(prog);
+  if (rc != SV_OK) {
+    delete prog;
+    return rc;
+  }
+  *out = prog;
+  return SV_OK;
+}
+
 }  // namespace sv
 
 using namespace sv;
@@ -720,58 +1008,11 @@ int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op*
   if (nqubits < kLowBits + kRB || nqubits > kMaxQubits)
     return set_error(SV_ERR_ARG, "fused programs need %d..%d qubits", kLowBits + kRB, kMaxQubits);
   if (nops < 0 || (nops > 0 && !ops)) return set_error(SV_ERR_ARG, "bad op list");
-  int kt = tile_bits;
-  if (kt <= 0) kt = dtype == SV_C128 ? 11 : 12;
-  if (kt > nqubits) kt = nqubits;
-  const int kt_max = kRB + (dtype == SV_C128 ? 8 : 9);
-  if (kt < kLowBits + kRB || kt > kt_max)
-    return set_error(SV_ERR_ARG, "tile_bits must be in [%d, %d]", kLowBits + kRB, kt_max);
-  sv_program* prog = new sv_program();
-  prog->dtype = dtype;
-  prog->nqubits = nqubits;
-  prog->kt = kt;
-  for (int i = 0; i < nops; i++) {
-    const sv_gate_op& g = ops[i];
-    HostOp h;
-    h.kind = g.kind;
-    h.nt = g.ntargets;
-    h.nc = g.ncontrols;
-    const bool ok_kind = g.kind == SV_OP_DENSE || g.kind == SV_OP_DIAG;
-    if (!ok_kind || g.ntargets < 1 || g.ntargets > kMaxTargets || g.ncontrols < 0 || g.ncontrols > 16 ||
-        !g.matrix) {
-      delete prog;
-      return set_error(SV_ERR_ARG, "op %d: bad kind, target count, control count or matrix", i);
-    }
-    uint64_t seen = 0;
-    for (int k = 0; k < g.ntargets + g.ncontrols; k++) {
-      const int q = k < g.ntargets ? g.targets[k] : g.controls[k - g.ntargets];
-      if (q < 0 || q >= nqubits || ((seen >> q) & 1)) {
-        delete prog;
-        return set_error(SV_ERR_ARG, "op %d: qubit %d out of range or repeated", i, q);
-      }
-      seen |= 1ull << q;
-      if (k < g.ntargets) h.tpos[k] = nqubits - 1 - q;
-      else h.cpos[k - g.ntargets] = nqubits - 1 - q;
-    }
-    const size_t ne = g.kind == SV_OP_DENSE ? ((size_t)1 << (2 * g.ntargets)) : ((size_t)1 << g.ntargets);
-    h.m.assign(g.matrix, g.matrix + 2 * ne);
-    if (g.kind == SV_OP_DIAG) {
-      h.sign_only = true;
-      for (size_t e = 0; e < ne; e++) {
-        const double re = h.m[2 * e], im = h.m[2 * e + 1];
-        if (im != 0.0 || (re != 1.0 && re != -1.0)) h.sign_only = false;
-        if (re == -1.0 && im == 0.0) h.sign_mask |= 1 << e;
-      }
-    }
-    prog->ops.push_back(std::move(h));
-  }
-  const int rc = dtype == SV_C128 ? build_program<c128>(prog) : build_program<c64>(prog);
-  if (rc != SV_OK) {
-    delete prog;
-    return rc;
-  }
-  *out = prog;
-  return SV_OK;
+  int kt = 0;
+  SV_TRY(check_tile_bits(dtype, nqubits, tile_bits, &kt));
+  std::vector<HostOp> hops;
+  SV_TRY(parse_ops(nqubits, ops, nops, &hops));
+  return plan(dtype, nqubits, kt, std::move(hops), out);
 }
 
 int sv_program_run(sv_context* ctx, const sv_program* prog, void* state) {
@@ -791,6 +1032,416 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
 
 int sv_program_destroy(sv_program* prog) {
   delete prog;
+  return SV_OK;
+}
+
+}  // extern "C"
+
+// ============================================================ batched circuits
+// Thousands of circuits of uneven size run together: circuits with the same gate
+// structure (same qubit count, same gates on the same qubits) form a group that is
+// planned once; each circuit gets its own coefficient block gathered through the
+// plan's coefficient-source map.  One run = zero all states, then every pass of every
+// group as one batched launch (circuits x tiles), groups spread over several streams.
+// The first run executes eagerly and records a CUDA graph of the same launches;
+// later runs replay the graph.
+namespace sv {
+
+constexpr int kBatchStreams = 4;
+
+struct BatchGroup {
+  sv_program* prog = nullptr;
+  std::vector<int> circuits;
+  void* d_coef = nullptr;      // ncirc x coef_total elements
+  void* d_states = nullptr;    // ncirc device pointers
+};
+
+}  // namespace sv
+
+struct sv_batch {
+  int dtype = 0, ncirc = 0, kt = 0;
+  std::vector<int> nq;
+  std::vector<size_t> off;             // element offset of each circuit's state
+  size_t total = 0;                    // elements
+  void* d_buf = nullptr;
+  void* d_ptrs = nullptr;              // ncirc state pointers (for the ones kernel / energies)
+  std::vector<std::vector<sv::HostOp>> ops;
+  std::vector<sv::BatchGroup> groups;
+  cudaStream_t streams[sv::kBatchStreams] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[sv::kBatchStreams] = {};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // energies
+  int nblocks = 0;
+  void* d_blocks = nullptr;            // int2 (circuit, block index within circuit) per energy block
+  void* d_nb = nullptr;                // blocks per circuit
+  double* d_partials = nullptr;
+  double* d_energy = nullptr;
+  double* h_energy = nullptr;          // pinned
+};
+
+namespace sv {
+
+template <typename T>
+__global__ void k_batch_ones(T* const* states, int ncirc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncirc) return;
+  if constexpr (is_complex<T>::value) {
+    using R = typename real_of<T>::type;
+    states[c][0] = T{(R)1, (R)0};
+  } else {
+    states[c][0] = (T)1;
+  }
+}
+
+// TFIM energy E = -sum_i <Z_i Z_{i+1}> - h sum_i <X_i> (open chain), per circuit.
+// Amplitude k contributes -(n-1-2*popc((k ^ k>>1) & (2^(n-1)-1))) |a_k|^2 for the ZZ
+// terms and -2h sum_{b: bit b of k is 0} Re(conj(a_k) a_{k | 2^b}) for the X terms.
+template <typename T>
+__global__ void __launch_bounds__(256) k_tfim_partials(T* const* states, const int* nqs, const int2* blocks,
+                                                      const int* nb, double h, double* partials) {
+  const int2 bi = blocks[blockIdx.x];
+  const int c = bi.x;
+  const int n = nqs[c];
+  const T* s = states[c];
+  const int64_t N = (int64_t)1 << n;
+  const int64_t stride = (int64_t)nb[c] * blockDim.x;
+  const int64_t zzmask = (N >> 1) - 1;
+  double acc = 0.0;
+  for (int64_t k = (int64_t)bi.y * blockDim.x + threadIdx.x; k < N; k += stride) {
+    const T a = s[k];
+    double ar, ai;
+    if constexpr (is_complex<T>::value) { ar = (double)a.re; ai = (double)a.im; } else { ar = (double)a; ai = 0.0; }
+    using R = typename real_of<T>::type;
+    R xs = 0;
+    for (int b = 0; b < n; b++) {
+      const int64_t kb = k | ((int64_t)1 << b);
+      if (kb == k) continue;
+      const T q = s[kb];
+      if constexpr (is_complex<T>::value) xs += a.re * q.re + a.im * q.im;
+      else xs += a * q;
+    }
+    const int zz = (n - 1) - 2 * __popcll((unsigned long long)((k ^ (k >> 1)) & zzmask));
+    acc += -(double)zz * (ar * ar + ai * ai) - 2.0 * h * (double)xs;
+  }
+  // block sum (fixed order)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double part[8];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += part[w];
+    partials[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_tfim_finish(const double* partials, const int* nb, const int* first, int ncirc, double* energy) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncirc) return;
+  double s = 0.0, comp = 0.0;
+  for (int i = 0; i < nb[c]; i++) {
+    const double x = partials[first[c] + i];
+    const double t = s + x;
+    comp += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  energy[c] = s + comp;
+}
+
+static bool same_structure(const std::vector<HostOp>& a, const std::vector<HostOp>& b) {
+  if (a.size() != b.size()) return false;
+  for (size_t i = 0; i < a.size(); i++) {
+    const HostOp& x = a[i];
+    const HostOp& y = b[i];
+    if (x.kind != y.kind || x.nt != y.nt || x.nc != y.nc || x.sign_only != y.sign_only ||
+        (x.sign_only && x.sign_mask != y.sign_mask) || x.is_x != y.is_x || x.is_real != y.is_real ||
+        x.is_swap != y.is_swap)
+      return false;
+    for (int k = 0; k < x.nt; k++)
+      if (x.tpos[k] != y.tpos[k]) return false;
+    for (int k = 0; k < x.nc; k++)
+      if (x.cpos[k] != y.cpos[k]) return false;
+  }
+  return true;
+}
+
+template <typename T>
+static int batch_build(sv_batch* b) {
+  // coefficient blocks and state pointer tables per group
+  for (auto& g : b->groups) {
+    const sv_program* prog = g.prog;
+    const size_t nc = g.circuits.size(), ct = prog->coef_total;
+    std::vector<T> coef(nc * ct);
+    std::vector<T*> ptrs(nc);
+    for (size_t i = 0; i < nc; i++) {
+      const int c = g.circuits[i];
+      const std::vector<HostOp>& ops = b->ops[c];
+      for (size_t sl = 0; sl < ct; sl++) {
+        const int op = prog->coef_src[2 * sl], e = prog->coef_src[2 * sl + 1];
+        coef[i * ct + sl] = to_elem<T>(&ops[op].m[2 * e]);
+      }
+      ptrs[i] = (T*)b->d_buf + b->off[c];
+    }
+    if (ct) {
+      SV_TRY(check_cuda(cudaMalloc(&g.d_coef, nc * ct * sizeof(T)), "batch coefficients"));
+      SV_TRY(check_cuda(cudaMemcpy(g.d_coef, coef.data(), nc * ct * sizeof(T), cudaMemcpyHostToDevice), "coef upload"));
+    }
+    SV_TRY(check_cuda(cudaMalloc(&g.d_states, nc * sizeof(T*)), "batch pointers"));
+    SV_TRY(check_cuda(cudaMemcpy(g.d_states, ptrs.data(), nc * sizeof(T*), cudaMemcpyHostToDevice), "pointer upload"));
+  }
+  std::vector<T*> all(b->ncirc);
+  for (int c = 0; c < b->ncirc; c++) all[c] = (T*)b->d_buf + b->off[c];
+  SV_TRY(check_cuda(cudaMalloc(&b->d_ptrs, b->ncirc * sizeof(T*)), "batch pointers"));
+  SV_TRY(check_cuda(cudaMemcpy(b->d_ptrs, all.data(), b->ncirc * sizeof(T*), cudaMemcpyHostToDevice), "pointer upload"));
+  return SV_OK;
+}
+
+template <typename T>
+static int batch_launches(Context* ctx, sv_batch* b) {
+  const size_t bytes = b->total * sizeof(T);
+  SV_TRY(check_cuda(cudaMemsetAsync(b->d_buf, 0, bytes, b->streams[0]), "batch zero"));
+  k_batch_ones<T><<<grid_for(b->ncirc, 256), 256, 0, b->streams[0]>>>((T* const*)b->d_ptrs, b->ncirc);
+  SV_LAUNCH_CHECK("batch ones");
+  SV_TRY(check_cuda(cudaEventRecord(b->ev_fork, b->streams[0]), "fork"));
+  for (int k = 1; k < kBatchStreams; k++)
+    SV_TRY(check_cuda(cudaStreamWaitEvent(b->streams[k], b->ev_fork, 0), "fork wait"));
+  // largest groups first, round-robin over the streams
+  for (size_t gi = 0; gi < b->groups.size(); gi++) {
+    const BatchGroup& g = b->groups[gi];
+    const sv_program* prog = g.prog;
+    cudaStream_t st = b->streams[gi % kBatchStreams];
+    const int kt = prog->kt;
+    const int threads = 1 << (kt - kRB);
+    const size_t smem = pass_smem<T>(kt);
+    BatchArgs<T> args;
+    memset(&args, 0, sizeof(args));
+    args.states = (T* const*)g.d_states;
+    args.coef = (const T*)g.d_coef;
+    args.coef_stride = (int64_t)prog->coef_total;
+    args.ncirc = (int32_t)g.circuits.size();
+    for (const Segment& s : prog->segments) {
+      const PassParams<T>& p =
+          *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
+      SV_TRY(launch_pass<T, true>(ctx, p, nullptr, threads, smem, p.ntiles * args.ncirc, st, args));
+    }
+  }
+  for (int k = 1; k < kBatchStreams; k++) {
+    SV_TRY(check_cuda(cudaEventRecord(b->ev_join[k], b->streams[k]), "join"));
+    SV_TRY(check_cuda(cudaStreamWaitEvent(b->streams[0], b->ev_join[k], 0), "join wait"));
+  }
+  return SV_OK;
+}
+
+static void batch_free(sv_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto& g : b->groups) {
+    if (g.d_coef) cudaFree(g.d_coef);
+    if (g.d_states) cudaFree(g.d_states);
+    delete g.prog;
+  }
+  for (int k = 0; k < kBatchStreams; k++) {
+    if (b->streams[k]) cudaStreamDestroy(b->streams[k]);
+    if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);
+  }
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->d_buf) cudaFree(b->d_buf);
+  if (b->d_ptrs) cudaFree(b->d_ptrs);
+  if (b->d_blocks) cudaFree(b->d_blocks);
+  if (b->d_nb) cudaFree(b->d_nb);
+  if (b->d_partials) cudaFree(b->d_partials);
+  if (b->d_energy) cudaFree(b->d_energy);
+  if (b->h_energy) cudaFreeHost(b->h_energy);
+  delete b;
+}
+
+}  // namespace sv
+
+extern "C" {
+
+int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubits, const sv_gate_op* const* ops,
+                    const int32_t* nops, int tile_bits, sv_batch** out) {
+  if (!ctx || !out || !nqubits || !ops || !nops || ncirc < 1) return set_error(SV_ERR_ARG, "bad batch arguments");
+  *out = nullptr;
+  if (dtype != SV_C128 && dtype != SV_C64) return set_error(SV_ERR_UNSUPPORTED, "batches need a complex dtype");
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  sv_batch* b = new sv_batch();
+  b->dtype = dtype;
+  b->ncirc = ncirc;
+  const size_t es = dtype_size(dtype);
+  // parse every circuit through the program front end (validation included)
+  std::vector<sv_program*> progs(ncirc, nullptr);
+  for (int c = 0; c < ncirc; c++) {
+    const int n = nqubits[c];
+    if (n < kLowBits + kRB || n > 34) {
+      batch_free(b);
+      return set_error(SV_ERR_ARG, "circuit %d: %d qubits outside [%d, 34]", c, n, kLowBits + kRB);
+    }
+    b->nq.push_back(n);
+    b->off.push_back(b->total);
+    b->total += ((((size_t)1 << n) * es + 255) / 256) * 256 / es;
+  }
+  // groups: identical structure (after single-qubit merging); plan one circuit per group
+  for (int c = 0; c < ncirc; c++) {
+    std::vector<HostOp> hops;
+    int rc = parse_ops(nqubits[c], ops[c], nops[c], &hops);
+    int kt = 0;
+    if (rc == SV_OK) rc = check_tile_bits(dtype, nqubits[c], tile_bits, &kt);
+    if (rc != SV_OK) {
+      batch_free(b);
+      return rc;
+    }
+    bool found = false;
+    for (auto& g : b->groups) {
+      if (g.prog->nqubits == nqubits[c] && g.prog->kt == kt && same_structure(g.prog->ops, hops)) {
+        g.circuits.push_back(c);
+        found = true;
+        break;
+      }
+    }
+    b->ops.push_back(hops);
+    if (!found) {
+      sv_program* p = nullptr;
+      rc = plan(dtype, nqubits[c], kt, std::move(hops), &p);
+      if (rc == SV_OK && p->nunfused) {
+        sv_program_destroy(p);
+        rc = set_error(SV_ERR_UNSUPPORTED, "circuit %d has gates on more than 2 targets; batches need fusable gates", c);
+      }
+      if (rc != SV_OK) {
+        batch_free(b);
+        return rc;
+      }
+      BatchGroup g;
+      g.prog = p;
+      g.circuits.push_back(c);
+      b->groups.push_back(g);
+    }
+  }
+  // largest states first so the big groups start early on every stream
+  std::stable_sort(b->groups.begin(), b->groups.end(), [](const BatchGroup& x, const BatchGroup& y) {
+    return ((size_t)x.circuits.size() << x.prog->nqubits) > ((size_t)y.circuits.size() << y.prog->nqubits);
+  });
+  int rc = check_cuda(cudaMalloc(&b->d_buf, b->total * es), "batch states");
+  if (rc == SV_OK) rc = dtype == SV_C128 ? batch_build<c128>(b) : batch_build<c64>(b);
+  for (int k = 0; k < kBatchStreams && rc == SV_OK; k++) {
+    rc = check_cuda(cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking), "batch stream");
+    if (rc == SV_OK) rc = check_cuda(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming), "event");
+  }
+  if (rc == SV_OK) rc = check_cuda(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
+  // energy block table: up to 64 blocks of 256 threads per circuit
+  if (rc == SV_OK) {
+    std::vector<int2> blocks;
+    std::vector<int> nb(ncirc), first(ncirc);
+    for (int c = 0; c < ncirc; c++) {
+      int64_t want = ((int64_t)1 << b->nq[c]) / 4096;
+      if (want < 1) want = 1;
+      if (want > 64) want = 64;
+      nb[c] = (int)want;
+      first[c] = (int)blocks.size();
+      for (int k = 0; k < nb[c]; k++) blocks.push_back(make_int2(c, k));
+    }
+    b->nblocks = (int)blocks.size();
+    rc = check_cuda(cudaMalloc(&b->d_blocks, blocks.size() * sizeof(int2)), "energy table");
+    if (rc == SV_OK) rc = check_cuda(cudaMalloc(&b->d_nb, 3 * ncirc * sizeof(int)), "energy table");
+    if (rc == SV_OK) rc = check_cuda(cudaMalloc(&b->d_partials, blocks.size() * sizeof(double)), "energy partials");
+    if (rc == SV_OK) rc = check_cuda(cudaMalloc(&b->d_energy, ncirc * sizeof(double)), "energies");
+    if (rc == SV_OK) rc = check_cuda(cudaMallocHost(&b->h_energy, ncirc * sizeof(double)), "energies (host)");
+    if (rc == SV_OK)
+      rc = check_cuda(cudaMemcpy(b->d_blocks, blocks.data(), blocks.size() * sizeof(int2), cudaMemcpyHostToDevice),
+                      "energy table upload");
+    if (rc == SV_OK) {
+      std::vector<int> nbf(nb);  // [blocks per circuit | first block | qubits]
+      nbf.insert(nbf.end(), first.begin(), first.end());
+      nbf.insert(nbf.end(), b->nq.begin(), b->nq.end());
+      rc = check_cuda(cudaMemcpy(b->d_nb, nbf.data(), nbf.size() * sizeof(int), cudaMemcpyHostToDevice), "upload");
+    }
+  }
+  if (rc != SV_OK) {
+    batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return SV_OK;
+}
+
+int sv_batch_run(sv_context* ctx, sv_batch* b) {
+  if (!ctx || !b) return set_error(SV_ERR_ARG, "null context or batch");
+  cudaEvent_t ev;
+  SV_TRY(check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event"));
+  // order after earlier work on the context stream
+  SV_TRY(check_cuda(cudaEventRecord(ev, ctx->stream), "event"));
+  SV_TRY(check_cuda(cudaStreamWaitEvent(b->streams[0], ev, 0), "wait"));
+  int rc = SV_OK;
+  if (b->exec) {
+    rc = check_cuda(cudaGraphLaunch(b->exec, b->streams[0]), "graph launch");
+  } else {
+    // first run: eager (sets kernel attributes), then record the same launches as a graph
+    rc = b->dtype == SV_C128 ? batch_launches<c128>(ctx, b) : batch_launches<c64>(ctx, b);
+    if (rc == SV_OK) rc = check_cuda(cudaStreamSynchronize(b->streams[0]), "batch sync");
+    if (rc == SV_OK) rc = check_cuda(cudaStreamBeginCapture(b->streams[0], cudaStreamCaptureModeThreadLocal), "capture");
+    if (rc == SV_OK) {
+      const int rc2 = b->dtype == SV_C128 ? batch_launches<c128>(ctx, b) : batch_launches<c64>(ctx, b);
+      cudaGraph_t g = nullptr;
+      const int rc3 = check_cuda(cudaStreamEndCapture(b->streams[0], &g), "end capture");
+      rc = rc2 != SV_OK ? rc2 : rc3;
+      if (rc == SV_OK) {
+        b->graph = g;
+        rc = check_cuda(cudaGraphInstantiate(&b->exec, g, 0), "graph instantiate");
+      } else if (g) {
+        cudaGraphDestroy(g);
+      }
+    }
+    // the eager run already produced the states; the graph is for later runs
+  }
+  if (rc == SV_OK) rc = check_cuda(cudaEventRecord(ev, b->streams[0]), "event");
+  if (rc == SV_OK) rc = check_cuda(cudaStreamWaitEvent(ctx->stream, ev, 0), "wait");
+  cudaEventDestroy(ev);
+  return rc;
+}
+
+int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energies) {
+  if (!ctx || !b || !energies) return set_error(SV_ERR_ARG, "null argument");
+  const int* nb = (const int*)b->d_nb;
+  const int* first = nb + b->ncirc;
+  const int* nqs = nb + 2 * b->ncirc;
+  if (b->dtype == SV_C128)
+    k_tfim_partials<c128><<<b->nblocks, 256, 0, ctx->stream>>>((c128* const*)b->d_ptrs, nqs, (const int2*)b->d_blocks,
+                                                               nb, h, b->d_partials);
+  else
+    k_tfim_partials<c64><<<b->nblocks, 256, 0, ctx->stream>>>((c64* const*)b->d_ptrs, nqs, (const int2*)b->d_blocks,
+                                                              nb, h, b->d_partials);
+  SV_LAUNCH_CHECK("tfim energy launch");
+  k_tfim_finish<<<grid_for(b->ncirc, 128), 128, 0, ctx->stream>>>(b->d_partials, nb, first, b->ncirc, b->d_energy);
+  SV_LAUNCH_CHECK("tfim finish launch");
+  SV_TRY(check_cuda(cudaMemcpyAsync(b->h_energy, b->d_energy, b->ncirc * sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->stream), "energy copy"));
+  SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "energy sync"));
+  memcpy(energies, b->h_energy, b->ncirc * sizeof(double));
+  return SV_OK;
+}
+
+int sv_batch_state(const sv_batch* b, int circuit, void** state, int* nqubits) {
+  if (!b || circuit < 0 || circuit >= b->ncirc || !state) return set_error(SV_ERR_ARG, "bad batch query");
+  *state = (unsigned char*)b->d_buf + b->off[circuit] * dtype_size(b->dtype);
+  if (nqubits) *nqubits = b->nq[circuit];
+  return SV_OK;
+}
+
+int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_bytes) {
+  if (!b) return set_error(SV_ERR_ARG, "null batch");
+  int np = 0;
+  for (auto& g : b->groups) np += g.prog->npasses;
+  if (ngroups) *ngroups = (int)b->groups.size();
+  if (npasses) *npasses = np;
+  if (state_bytes) *state_bytes = b->total * dtype_size(b->dtype);
+  return SV_OK;
+}
+
+int sv_batch_destroy(sv_batch* b) {
+  batch_free(b);
   return SV_OK;
 }
 

@@ -1,0 +1,63 @@
+"""Batched circuits (config: many hardware-efficient-ansatz circuits of uneven size)."""
+import numpy as np
+import pytest
+
+from qibojit_gb300.batch import BatchedCircuits, hea_batch, hea_circuit, tfim_energy_dense
+from tests.circuits_random import random_circuit
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def backend():
+    from qibojit_gb300 import MetaBackend
+
+    return MetaBackend.load("gb300")
+
+
+@pytest.mark.parametrize("dt,tol", [("complex128", 1e-12), ("complex64", 2e-5)])
+def test_hea_batch_matches_single_circuits(backend, dt, tol):
+    dtype = dt
+    specs = hea_batch(40, seed=5, nmin=8, nmax=15, lmin=2, lmax=5)
+    circs = [hea_circuit(n, L, p) for n, L, p in specs]
+    batch = BatchedCircuits(backend, circs, dtype)
+    st = batch.stats()
+    assert st["groups"] <= len(circs)
+    batch.run()
+    energies = batch.tfim_energies(1.0)
+    for i, c in enumerate(circs):
+        got = backend.to_numpy(batch.state(i))
+        want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits, dtype=dtype), fuse=False))
+        np.testing.assert_allclose(got, want, rtol=0, atol=tol)
+        e = tfim_energy_dense(want, c.nqubits, 1.0)
+        assert abs(energies[i] - e) < (1e-11 if dtype == "complex128" else 1e-4) * max(1.0, abs(e))
+
+
+def test_batch_graph_replay_is_repeatable(backend):
+    specs = hea_batch(64, seed=9, nmin=8, nmax=16, lmin=2, lmax=6)
+    batch = BatchedCircuits(backend, [hea_circuit(n, L, p) for n, L, p in specs], "complex64")
+    batch.run()                      # eager run + graph capture
+    e1 = batch.tfim_energies()
+    batch.run()                      # graph replay
+    e2 = batch.tfim_energies()
+    batch.run()
+    e3 = batch.tfim_energies()
+    np.testing.assert_array_equal(e1, e2)
+    np.testing.assert_array_equal(e2, e3)
+
+
+def test_batch_of_random_circuits(backend):
+    """Arbitrary fusable gates (1-2 targets, controls) in a batch, two structures repeated."""
+    from qibojit_gb300 import gates as G
+
+    circs = []
+    for k in range(6):
+        c = random_circuit(10 + (k % 2), 40, seed=100 + k % 2,
+                           families=["one", "one_p", "two_c", "two_p", "swap", "fsim", "u2q", "zc", "ccz", "toffoli"])
+        circs.append(c)
+    batch = BatchedCircuits(backend, circs, "complex128")
+    assert batch.stats()["groups"] == 2
+    batch.run()
+    for i, c in enumerate(circs):
+        want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits), fuse=False))
+        np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want, rtol=0, atol=1e-12)

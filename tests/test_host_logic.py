@@ -1,0 +1,97 @@
+"""Host-side logic that needs no GPU: gate matrices, fused-gate matrices, circuit
+builders and the reference energy formula."""
+import numpy as np
+import pytest
+
+from qibojit_gb300 import circuits
+from qibojit_gb300 import gates as G
+from qibojit_gb300.batch import hea_batch, hea_circuit, tfim_energy_dense
+from qibojit_gb300.fusion import SV_OP_DENSE, SV_OP_DIAG, lower, matrix_fused
+from qibojit_gb300.matrices import CustomMatrices, Matrices
+from tests.dense import apply_dense, random_state
+
+
+def test_matrices_are_unitary():
+    m = Matrices()
+    rng = np.random.default_rng(0)
+    for name in ["H", "X", "Y", "Z", "S", "SDG", "T", "TDG", "SX", "SXDG", "CNOT", "CZ", "SWAP", "TOFFOLI", "CCZ"]:
+        u = getattr(m, name)
+        np.testing.assert_allclose(u @ u.conj().T, np.eye(u.shape[0]), atol=1e-14)
+    for name, k in [("RX", 1), ("RY", 1), ("RZ", 1), ("U1", 1), ("U2", 2), ("U3", 3), ("fSim", 2), ("CU3", 3)]:
+        u = getattr(m, name)(*rng.uniform(0, 2 * np.pi, k))
+        np.testing.assert_allclose(u @ u.conj().T, np.eye(u.shape[0]), atol=1e-14)
+
+
+def test_u3_conventions():
+    m = Matrices()
+    # U3(t, -pi/2, pi/2) = RX(t); U3(t, 0, 0) = RY(t); U3(0, 0, l) = RZ(l) up to phase conventions
+    t = 0.7
+    np.testing.assert_allclose(m.U3(t, -np.pi / 2, np.pi / 2), m.RX(t), atol=1e-15)
+    np.testing.assert_allclose(m.U3(t, 0, 0), m.RY(t), atol=1e-15)
+    np.testing.assert_allclose(m.U3(0, 0, 0.3), m.RZ(0.3), atol=1e-15)
+
+
+def test_custom_operands():
+    cm = CustomMatrices()
+    assert cm.U1(0.4).shape == ()
+    assert np.isclose(cm.U1(0.4), np.exp(0.4j))
+    f = cm.fSim(0.3, 0.2)
+    assert f.shape == (5,) and np.isclose(f[4], np.exp(-0.2j))
+    np.testing.assert_allclose(cm.CNOT, Matrices().X)
+
+
+def test_lower_classifies_diagonals():
+    c = G.Circuit(3)
+    c.add([G.RZ(0, theta=0.1), G.CZ(0, 1), G.RY(1, theta=0.2), G.CNOT(1, 2), G.U1(2, theta=0.3)])
+    kinds = [k for k, *_ in lower(c.queue)]
+    assert kinds == [SV_OP_DIAG, SV_OP_DIAG, SV_OP_DENSE, SV_OP_DENSE, SV_OP_DIAG]
+
+
+def test_matrix_fused_matches_sequential_application():
+    rng = np.random.default_rng(1)
+    n = 4
+    fg = G.FusedGate(0, 1, 3)
+    for g in [G.U3(0, *rng.uniform(0, 6, 3)), G.CNOT(3, 1), G.RY(1, theta=0.4), G.CZ(0, 3), G.SWAP(0, 3)]:
+        fg.append(g)
+    x = random_state(n, 2)
+    want = x.copy()
+    for g in fg.gates:
+        want = apply_dense(want, g.base_matrix(), list(g.target_qubits), list(g.control_qubits), n)
+    got = apply_dense(x, matrix_fused(fg), [0, 1, 3], [], n)
+    np.testing.assert_allclose(got, want, atol=1e-14)
+
+
+def test_brickwork_and_qft_shapes():
+    c = circuits.brickwork(30, 20, 1234)
+    assert len(c.queue) == 890
+    assert sum(type(g).__name__ == "U3" for g in c.queue) == 600
+    q = circuits.qft(20)
+    assert len(q.queue) == 20 + 190 + 10
+
+
+def test_hea_batch_distribution():
+    specs = hea_batch(4096, seed=1234)
+    ns = np.array([s[0] for s in specs])
+    ls = np.array([s[1] for s in specs])
+    assert ns.min() == 10 and ns.max() == 22 and ls.min() == 4 and ls.max() == 12
+    n, L, p = specs[0]
+    assert len(hea_circuit(n, L, p).queue) == L * (3 * n - 1)
+
+
+@pytest.mark.parametrize("n", [2, 3, 5])
+def test_tfim_energy_dense_matches_hamiltonian_matrix(n):
+    I2, X, Z = np.eye(2), np.array([[0, 1], [1, 0]]), np.diag([1.0, -1.0])
+
+    def op(single, q):
+        out = np.array([[1.0]])
+        for k in range(n):
+            out = np.kron(out, single if k == q else I2)
+        return out
+
+    H = np.zeros((2**n, 2**n))
+    for i in range(n - 1):
+        H -= op(Z, i) @ op(Z, i + 1)
+    for i in range(n):
+        H -= 0.7 * op(X, i)
+    x = random_state(n, 3)
+    assert abs(tfim_energy_dense(x, n, 0.7) - np.real(np.vdot(x, H @ x))) < 1e-13
