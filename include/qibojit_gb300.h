@@ -226,6 +226,29 @@ int sv_batch_state(const sv_batch* b, int circuit, void** state, int* nqubits);
 int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_bytes);
 int sv_batch_destroy(sv_batch* b);
 
+/* ---------------------------------------------------------- adjoint gradients */
+/* Gradients of the transverse-field Ising energy E = <psi|H|psi>,
+ * H = -sum_i Z_i Z_{i+1} - h sum_i X_i, for `ncirc` circuits of one structure (same
+ * gates on the same qubits, different parameters) by the adjoint method.  Gate j is a
+ * fixed gate (generators[j] = 0) or exp(-i t G / 2) with G = X, Y, Z (generators[j] =
+ * 1, 2, 3) on one qubit, t = parameter params[j] in [0, nparams).  The forward state is
+ * checkpointed after segment_ends[0..nsegments-2] and restored during the reverse
+ * sweep (bounds complex64 drift); inner products accumulate in FP64.  The reference
+ * has no gradient path; this extends it for variational workloads. */
+typedef struct sv_adjoint sv_adjoint;
+int sv_adjoint_create(sv_context* ctx, int dtype, int ncirc, int nqubits, const sv_gate_op* const* ops, int nops,
+                      const int8_t* generators, const int32_t* params, int nparams, const int32_t* segment_ends,
+                      int nsegments, int tile_bits, sv_adjoint** out);
+/* New parameters for the same structure: re-gathers coefficients, keeps plans and memory. */
+int sv_adjoint_update(sv_context* ctx, sv_adjoint* A, const sv_gate_op* const* ops, int nops,
+                      const int8_t* generators, const int32_t* params);
+/* Forward + reverse sweep: energies (host, ncirc) and gradients (host, ncirc x nparams,
+ * row-major); either may be NULL.  Synchronises. */
+int sv_adjoint_run(sv_context* ctx, sv_adjoint* A, double h, double* energies, double* grads);
+/* Device pointer of a circuit's final forward state (valid after a run, until the next). */
+int sv_adjoint_state(const sv_adjoint* A, int circuit, void** psi);
+int sv_adjoint_destroy(sv_adjoint* A);
+
 #ifdef __cplusplus
 }
 #endif

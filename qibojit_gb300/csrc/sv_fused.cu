@@ -43,8 +43,13 @@ enum : uint8_t {
   FOP_D1RUN = 4,    // up to 4 uncontrolled complex 2x2 on distinct register bits
   FOP_X1 = 5,       // X (CNOT, Toffoli targets): a register swap, no arithmetic
   FOP_DENSE1R = 6,  // real 2x2 (RY, H): half the flops of a complex one
-  FOP_SWAP2 = 7     // SWAP: exchange of |01> and |10>, no arithmetic
+  FOP_SWAP2 = 7,    // SWAP: exchange of |01> and |10>, no arithmetic
+  FOP_GRADX = 8,    // adjoint sweep: Im<lambda|X_q|psi> on a register bit (coef = parameter index)
+  FOP_GRADY = 9,    //                Im<lambda|Y_q|psi>
+  FOP_GRADZ = 10    //                Im<lambda|Z_q|psi>, any bit (diagonal)
 };
+// internal op kind of the adjoint planner: a gradient marker (no matrix)
+constexpr int OP_GRAD = 2;
 enum : uint8_t { FLAG_OMASK = 1, FLAG_TMASK = 2 };
 
 // One op in phase-local form (64 bytes).
@@ -428,7 +433,12 @@ struct HostOp {
   bool is_x = false;        // dense one-target [[0, 1], [1, 0]]
   bool is_real = false;     // dense with all-real entries
   bool is_swap = false;     // dense two-target SWAP
+  int gen = 0;              // OP_GRAD: generator 1 = X, 2 = Y, 3 = Z
+  int param = -1;           // OP_GRAD: parameter index
 };
+
+// ops that need their target bit in the tile and in the phase's registers
+static inline bool dense_like(const HostOp& h) { return h.kind == SV_OP_DENSE || (h.kind == OP_GRAD && h.gen != 3); }
 
 struct Segment {
   bool fused = false;
@@ -464,6 +474,7 @@ static T to_elem(const double* re_im) {
 }
 
 static int coef_cost(const HostOp& h) {
+  if (h.kind == OP_GRAD) return 0;
   if (h.kind == SV_OP_DENSE) {
     if (h.is_x || (h.nt == 2 && h.is_swap)) return 0;
     return h.nt == 1 ? 4 : 16;
@@ -506,7 +517,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
   for (int oi : sched) {
     const HostOp& h = prog->ops[oi];
     Pending pd{oi, {-1, -1}};
-    if (h.kind == SV_OP_DENSE) {
+    if (dense_like(h)) {
       for (int i = 0; i < h.nt; i++) pd.lt[i] = local_of[h.tpos[i]];
       int need = 0;
       for (int i = 0; i < h.nt; i++)
@@ -518,7 +529,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
     cur.push_back(pd);
   }
   flush();
-  int nops = 0, ncoef = 0;
+  int nops = 0, ncoef = 0, ngrad = 0;
   for (size_t g = 0; g < groups.size(); g++) {
     std::vector<int> rb = group_bits[g];
     for (int b = kt - 1; b >= 0 && (int)rb.size() < kRB; b--)
@@ -550,7 +561,35 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
       }
       unsigned jm = 0;
       unsigned tbits = 0;  // register bits that are targets of a dense op
-      if (h.kind == SV_OP_DENSE) {
+      if (h.kind == OP_GRAD && h.gen != 3) {
+        f.type = h.gen == 1 ? FOP_GRADX : FOP_GRADY;
+        f.u0 = (uint8_t)regpos[pd.lt[0]];
+        f.u1 = (uint8_t)(ngrad++);  // shared-memory accumulator slot
+        f.coef = (uint32_t)h.param;
+        f.jmask = 0xffffu;
+      } else if (h.kind == OP_GRAD) {
+        // Z generator: a one-bit "diagonal" read like FOP_DIAG's index bits
+        f.type = FOP_GRADZ;
+        f.u1 = (uint8_t)(ngrad++);
+        f.coef = (uint32_t)h.param;
+        f.nd = 1;
+        f.jmask = 0xffffu;
+        for (int i = 0; i < 3; i++) {
+          f.tb[i] = -1;
+          f.ob[i] = -1;
+        }
+        const int lb = local_of[h.tpos[0]];
+        uint64_t rpart = 0;
+        if (lb >= 0 && regpos[lb] >= 0) {
+          for (int j = 0; j < 16; j++)
+            if ((j >> regpos[lb]) & 1) rpart |= (uint64_t)1 << (4 * j);
+        } else if (lb >= 0) {
+          f.tb[0] = (int8_t)lb;
+        } else {
+          f.ob[0] = (int8_t)h.tpos[0];
+        }
+        f.rpart = rpart;
+      } else if (h.kind == SV_OP_DENSE) {
         if (h.nt == 1) f.type = h.is_x ? FOP_X1 : (h.is_real ? FOP_DENSE1R : FOP_DENSE1);
         else f.type = h.is_swap ? FOP_SWAP2 : FOP_DENSE2;
         f.u0 = (uint8_t)regpos[pd.lt[0]];
@@ -691,7 +730,8 @@ static int build_program(sv_program* prog) {
   std::vector<int> barriers;
   for (size_t i = 0; i < prog->ops.size(); i++) {
     const HostOp& h = prog->ops[i];
-    const bool fusable = (h.kind == SV_OP_DIAG && h.nt <= 3) || (h.kind == SV_OP_DENSE && h.nt <= 2);
+    const bool fusable =
+        (h.kind == SV_OP_DIAG && h.nt <= 3) || (h.kind == SV_OP_DENSE && h.nt <= 2) || h.kind == OP_GRAD;
     if (fusable) {
       runs.back().push_back((int)i);
     } else {
@@ -723,7 +763,7 @@ static int build_program(sv_program* prog) {
           next.push_back(oi);
           continue;
         }
-        if (h.kind == SV_OP_DENSE) {
+        if (dense_like(h)) {
           const uint64_t need = tbits & ~S;
           const int nneed = __builtin_popcountll(need);
           if (ssize + nneed > kt) {
@@ -980,6 +1020,7 @@ static int check_tile_bits(int dtype, int nqubits, int tile_bits, int* kt_out) {
 }
 
 static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out) {
+  if (kt > nqubits || kt < kLowBits + kRB) return set_error(SV_ERR_ARG, "tile of %d bits for %d qubits", kt, nqubits);
   sv_program* prog = new sv_program();
   prog->dtype = dtype;
   prog->nqubits = nqubits;
@@ -1442,6 +1483,687 @@ int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_
 
 int sv_batch_destroy(sv_batch* b) {
   batch_free(b);
+  return SV_OK;
+}
+
+}  // extern "C"
+
+// ============================================================ adjoint gradients
+// Gradients of E = <psi|H|psi> for circuits of gates exp(-i t G / 2) (G = X, Y, Z on
+// one qubit) plus fixed gates, by the adjoint method: forward, lambda = H psi, then a
+// reverse sweep that for every gate j (last to first) takes
+//   dE/dt_j = Im <lambda|G_j|psi>     (psi, lambda after gate j)
+// and then un-applies gate j from both psi and lambda.  The sweep is planned like any
+// program (gradient markers before each U^dagger) and runs as tile passes that keep
+// the psi and lambda tiles side by side in shared memory.  Inner products are reduced
+// per warp in FP32, then in FP64 per block into per-(circuit, parameter, block) slots
+// (fixed order: deterministic).  Forward states are checkpointed at segment
+// boundaries and restored during the sweep, which bounds complex64 drift.
+namespace sv {
+
+constexpr int kAdjMaxGrad = 128;  // gradient markers per pass
+
+template <typename T>
+struct AdjArgs {
+  T* const* psi;
+  T* const* lam;
+  const T* coef;
+  int64_t coef_stride;
+  double* gpart;        // [circuit][parameter][gstride]
+  int32_t ncirc, nparams, gstride, pad;
+};
+
+// products in the state's own precision (FP32 for complex64, FP64 for complex128);
+// block and circuit sums are FP64
+template <typename T>
+__device__ __forceinline__ typename real_of<T>::type im_cdot(T a, T b) {  // Im(conj(a) b)
+  if constexpr (is_complex<T>::value) return a.re * b.im - a.im * b.re;
+  else return 0;
+}
+template <typename T>
+__device__ __forceinline__ typename real_of<T>::type re_cdot(T a, T b) {  // Re(conj(a) b)
+  if constexpr (is_complex<T>::value) return a.re * b.re + a.im * b.im;
+  else return a * b;
+}
+
+template <typename T, int U, int GEN>
+__device__ __forceinline__ typename real_of<T>::type grad_pairs(const T (&v)[16], const T (&w)[16]) {
+  typename real_of<T>::type acc = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    const int k = j | (1 << U);
+    if (GEN == 1) acc += im_cdot(w[j], v[k]) + im_cdot(w[k], v[j]);   // X
+    else acc += re_cdot(w[k], v[j]) - re_cdot(w[j], v[k]);            // Y
+  }
+  return acc;
+}
+
+template <typename T, int GEN>
+__device__ __forceinline__ typename real_of<T>::type grad_dispatch(const T (&v)[16], const T (&w)[16], int u) {
+  switch (u) {
+    case 0: return grad_pairs<T, 0, GEN>(v, w);
+    case 1: return grad_pairs<T, 1, GEN>(v, w);
+    case 2: return grad_pairs<T, 2, GEN>(v, w);
+    default: return grad_pairs<T, 3, GEN>(v, w);
+  }
+}
+
+template <typename T, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_adjoint_pass(const __grid_constant__ PassParams<T> p,
+                                                           const __grid_constant__ AdjArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int kt = p.kt;
+  const int tsize = 1 << kt;
+  const int tstride = tsize + (tsize >> 4);
+  T* const bpsi = reinterpret_cast<T*>(smem_raw);      // two psi tiles
+  T* const blam = bpsi + 2 * tstride;                   // two lambda tiles
+  int64_t* dep_hi = reinterpret_cast<int64_t*>(blam + 2 * tstride);
+  const int nwarps = blockDim.x >> 5;
+  double* gacc = reinterpret_cast<double*>(dep_hi + (1 << (kt - kLowBits)));  // [slot][warp]
+  const int nhi = kt - kLowBits;
+  for (int h = threadIdx.x; h < (1 << nhi); h += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < nhi; b++)
+      if ((h >> b) & 1) o |= (int64_t)1 << p.tile_pos[kLowBits + b];
+    dep_hi[h] = o;
+  }
+  for (int i = threadIdx.x; i < kAdjMaxGrad * nwarps; i += blockDim.x) gacc[i] = 0.0;
+  __syncthreads();
+  const int nthreads = blockDim.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto issue_load = [&](int slot, int64_t it) {
+    const int64_t base = tile_origin(it & (p.ntiles - 1), p.tile_pos, kt);
+    const T* sp = a.psi[it >> (p.n - kt)];
+    const T* sl = a.lam[it >> (p.n - kt)];
+    for (int e = threadIdx.x; e < tsize; e += nthreads) {
+      const int64_t g = base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1));
+      cp_async<sizeof(T)>(bpsi + slot * tstride + smem_pos(e), sp + g);
+      cp_async<sizeof(T)>(blam + slot * tstride + smem_pos(e), sl + g);
+    }
+    cp_async_commit();
+  };
+  // write this block's accumulated gradients of one circuit and clear the slots
+  auto flush = [&](int circ) {
+    __syncthreads();
+    for (int o = threadIdx.x; o < p.nops; o += blockDim.x) {
+      const FOp& op = p.ops[o];
+      if (op.type != FOP_GRADX && op.type != FOP_GRADY && op.type != FOP_GRADZ) continue;
+      double sum = 0.0;
+      for (int w = 0; w < nwarps; w++) {
+        sum += gacc[op.u1 * nwarps + w];
+        gacc[op.u1 * nwarps + w] = 0.0;
+      }
+      a.gpart[((int64_t)circ * a.nparams + op.coef) * a.gstride + blockIdx.x] = sum;
+    }
+    __syncthreads();
+  };
+  const int64_t nitems = p.ntiles * a.ncirc;
+  const int tshift = p.n - kt;
+  int64_t t = blockIdx.x;
+  if (t < nitems) issue_load(0, t);
+  int cur = 0;
+  int cur_circ = -1;
+  for (; t < nitems; t += gridDim.x, cur ^= 1) {
+    const int circ = (int)(t >> tshift);
+    if (circ != cur_circ) {
+      if (cur_circ >= 0) flush(cur_circ);
+      cur_circ = circ;
+    }
+    T* tp = bpsi + cur * tstride;
+    T* tl = blam + cur * tstride;
+    const int64_t base = tile_origin(t & (p.ntiles - 1), p.tile_pos, kt);
+    const T* cbase = a.coef + (int64_t)circ * a.coef_stride + p.coef_goff;
+    const int64_t tn = t + gridDim.x;
+    if (tn < nitems) {
+      issue_load(cur ^ 1, tn);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    for (int ph = 0; ph < p.nphases; ph++) {
+      const Phase& P = p.phases[ph];
+      const int r0 = P.rb[0], r1 = P.rb[1], r2 = P.rb[2], r3 = P.rb[3];
+      int lbase = threadIdx.x;
+      lbase = ((lbase >> r0) << (r0 + 1)) | (lbase & ((1 << r0) - 1));
+      lbase = ((lbase >> r1) << (r1 + 1)) | (lbase & ((1 << r1) - 1));
+      lbase = ((lbase >> r2) << (r2 + 1)) | (lbase & ((1 << r2) - 1));
+      lbase = ((lbase >> r3) << (r3 + 1)) | (lbase & ((1 << r3) - 1));
+      const int sb = smem_pos(lbase);
+      T v[16], w[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        v[j] = tp[sb + P.soff[j]];
+        w[j] = tl[sb + P.soff[j]];
+      }
+      unsigned pending_neg = 0;
+      for (int o = P.op_begin; o < P.op_end; o++) {
+        const FOp& op = p.ops[o];
+        const int type = op.type;
+        if (type == FOP_GRADZ) {
+          // sign of each amplitude from its bit; invariant under pending negations
+          int tpb = 0;
+          if (op.tb[0] >= 0) tpb = (lbase >> op.tb[0]) & 1;
+          else if (op.ob[0] >= 0) tpb = (int)((base >> op.ob[0]) & 1);
+          typename real_of<T>::type acc = 0;
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int bit = (int)((op.rpart >> (4 * j)) & 1) | tpb;
+            const auto x = im_cdot(w[j], v[j]);
+            acc += bit ? -x : x;
+          }
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          if (lane == 0) gacc[op.u1 * nwarps + warp] += (double)acc;
+          continue;
+        }
+        if (pending_neg && type != FOP_SIGN && type != FOP_DIAG) {
+          apply_negations(v, pending_neg);
+          apply_negations(w, pending_neg);
+          pending_neg = 0;
+        }
+        if (type == FOP_GRADX || type == FOP_GRADY) {
+          auto acc = type == FOP_GRADX ? grad_dispatch<T, 1>(v, w, op.u0) : grad_dispatch<T, 2>(v, w, op.u0);
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          if (lane == 0) gacc[op.u1 * nwarps + warp] += (double)acc;
+          continue;
+        }
+        const int flags = op.flags;
+        if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
+        if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;
+        if (type == FOP_DENSE1) {
+          dense1_dispatch(v, cbase + op.coef, op.u0, op.jmask);
+          dense1_dispatch(w, cbase + op.coef, op.u0, op.jmask);
+        } else if (type == FOP_DENSE1R) {
+          dense1r_dispatch(v, cbase + op.coef, op.u0, op.jmask);
+          dense1r_dispatch(w, cbase + op.coef, op.u0, op.jmask);
+        } else if (type == FOP_X1) {
+          x1_dispatch(v, op.u0, op.jmask);
+          x1_dispatch(w, op.u0, op.jmask);
+        } else if (type == FOP_SWAP2) {
+          swap2_dispatch(v, op.u0, op.u1, op.jmask);
+          swap2_dispatch(w, op.u0, op.u1, op.jmask);
+        } else if (type == FOP_DENSE2) {
+          dense2_dispatch(v, cbase + op.coef, op.u0, op.u1, op.jmask);
+          dense2_dispatch(w, cbase + op.coef, op.u0, op.u1, op.jmask);
+        } else {
+          const int nd = op.nd;
+          int tpx = 0;
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            if (i >= nd) break;
+            if (op.tb[i] >= 0) tpx |= ((lbase >> op.tb[i]) & 1) << (nd - 1 - i);
+            else if (op.ob[i] >= 0) tpx |= (int)((base >> op.ob[i]) & 1) << (nd - 1 - i);
+          }
+          if (type == FOP_SIGN) {
+            pending_neg ^= op.neg[tpx];
+          } else {
+            const unsigned jm = op.jmask;
+            const uint64_t rp = op.rpart;
+            const T* c = cbase + op.coef;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              if (!((jm >> j) & 1u)) continue;
+              const int idx = (int)((rp >> (4 * j)) & 15) | tpx;
+              v[j] = tmul(c[idx], v[j]);
+              w[j] = tmul(c[idx], w[j]);
+            }
+          }
+        }
+      }
+      if (pending_neg) {
+        apply_negations(v, pending_neg);
+        apply_negations(w, pending_neg);
+      }
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        tp[sb + P.soff[j]] = v[j];
+        tl[sb + P.soff[j]] = w[j];
+      }
+      __syncthreads();
+    }
+    T* const sp = a.psi[circ];
+    T* const sl = a.lam[circ];
+    for (int e = threadIdx.x; e < tsize; e += nthreads) {
+      const int64_t g = base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1));
+      stg_stream(sp + g, tp[smem_pos(e)]);
+      stg_stream(sl + g, tl[smem_pos(e)]);
+    }
+    __syncthreads();
+  }
+  if (cur_circ >= 0) flush(cur_circ);
+}
+
+template <typename T>
+static size_t adjoint_smem(int kt, int threads) {
+  const int tsize = 1 << kt;
+  return 4 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits)) +
+         sizeof(double) * kAdjMaxGrad * (threads / 32);
+}
+
+// lambda = H psi for H = -sum_i Z_i Z_{i+1} - h sum_i X_i (open chain), all circuits
+template <typename T>
+__global__ void __launch_bounds__(256) k_tfim_apply(T* const* psi, T* const* lam, int n, int ncirc, double h) {
+  const int64_t N = (int64_t)1 << n;
+  const int64_t total = N * ncirc;
+  const int64_t zzmask = (N >> 1) - 1;
+  using R = typename real_of<T>::type;
+  const R hh = (R)h;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(idx >> n);
+    const int64_t k = idx & (N - 1);
+    const T* s = psi[c];
+    const T a = s[k];
+    const int zz = (n - 1) - 2 * __popcll((unsigned long long)((k ^ (k >> 1)) & zzmask));
+    T out;
+    if constexpr (is_complex<T>::value) {
+      R re = -(R)zz * a.re, im = -(R)zz * a.im;
+      for (int b = 0; b < n; b++) {
+        const T q = s[k ^ ((int64_t)1 << b)];
+        re -= hh * q.re;
+        im -= hh * q.im;
+      }
+      out = T{re, im};
+    } else {
+      R re = -(R)zz * a;
+      for (int b = 0; b < n; b++) re -= hh * s[k ^ ((int64_t)1 << b)];
+      out = re;
+    }
+    lam[c][k] = out;
+  }
+}
+
+// per-circuit <psi|lambda> real part, FP64 (block partials, then a fixed-order finish)
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_dot_partials(T* const* psi, T* const* lam, int n, int nb,
+                                                           double* partials) {
+  const int c = blockIdx.y;
+  const int64_t N = (int64_t)1 << n;
+  double acc = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < N; k += (int64_t)nb * blockDim.x)
+    acc += (double)re_cdot(psi[c][k], lam[c][k]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double part[8];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += part[w];
+    partials[(int64_t)c * nb + blockIdx.x] = r;
+  }
+}
+
+__global__ void k_rows_sum(const double* in, int64_t rows, int cols, double* out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  double s = 0.0, comp = 0.0;
+  for (int i = 0; i < cols; i++) {
+    const double x = in[r * cols + i];
+    const double t = s + x;
+    comp += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  out[r] = s + comp;
+}
+
+struct AdjSegment {
+  sv_program* fwd = nullptr;
+  sv_program* bwd = nullptr;
+  void* d_fcoef = nullptr;
+  void* d_bcoef = nullptr;
+};
+
+}  // namespace sv
+
+struct sv_adjoint {
+  int dtype = 0, ncirc = 0, n = 0, nparams = 0, kt = 0;
+  std::vector<sv::AdjSegment> segs;
+  std::vector<std::vector<sv::HostOp>> fops;      // per circuit, forward (after parsing, no merging)
+  std::vector<std::vector<sv::HostOp>> bops;      // per circuit per segment, backward lists (concatenated)
+  std::vector<int> seg_begin;                     // op index where each segment starts (+ end)
+  void* d_psi = nullptr;
+  void* d_lam = nullptr;
+  void* d_cp = nullptr;                           // (nseg - 1) checkpoints per circuit
+  void* d_ptrs = nullptr;                         // [psi ptrs | lam ptrs]
+  size_t stride = 0;                              // elements per state
+  double* d_gpart = nullptr;
+  double* d_grad = nullptr;
+  double* d_epart = nullptr;
+  double* d_energy = nullptr;
+  int gstride = 0;
+  int enb = 0;
+};
+
+namespace sv {
+
+static std::vector<HostOp> backward_list(const std::vector<HostOp>& fwd, int b, int e, const int8_t* gens,
+                                         const int32_t* params) {
+  std::vector<HostOp> out;
+  for (int j = e - 1; j >= b; j--) {
+    const HostOp& h = fwd[j];
+    if (gens && gens[j] > 0) {
+      HostOp g;
+      g.kind = OP_GRAD;
+      g.nt = 1;
+      g.tpos[0] = h.tpos[0];
+      g.nc = 0;
+      g.gen = gens[j];
+      g.param = params[j];
+      out.push_back(g);
+    }
+    // the inverse: conjugate transpose (diagonal: conjugate)
+    HostOp inv = h;
+    if (h.kind == SV_OP_DIAG) {
+      for (size_t k = 1; k < inv.m.size(); k += 2) inv.m[k] = -inv.m[k];
+    } else {
+      const int d = 1 << h.nt;
+      for (int r = 0; r < d; r++)
+        for (int c = 0; c < d; c++) {
+          inv.m[2 * (r * d + c)] = h.m[2 * (c * d + r)];
+          inv.m[2 * (r * d + c) + 1] = -h.m[2 * (c * d + r) + 1];
+        }
+    }
+    classify(inv);
+    out.push_back(inv);
+  }
+  return out;
+}
+
+template <typename T>
+static int gather_coef(const sv_program* prog, const std::vector<std::vector<HostOp>>& per_circ, void** d) {
+  const size_t nc = per_circ.size(), ct = prog->coef_total;
+  if (ct == 0) return SV_OK;
+  std::vector<T> coef(nc * ct);
+  for (size_t i = 0; i < nc; i++)
+    for (size_t sl = 0; sl < ct; sl++) {
+      const int op = prog->coef_src[2 * sl], e = prog->coef_src[2 * sl + 1];
+      coef[i * ct + sl] = to_elem<T>(&per_circ[i][op].m[2 * e]);
+    }
+  if (!*d) SV_TRY(check_cuda(cudaMalloc(d, nc * ct * sizeof(T)), "adjoint coefficients"));
+  return check_cuda(cudaMemcpy(*d, coef.data(), nc * ct * sizeof(T), cudaMemcpyHostToDevice), "coef upload");
+}
+
+template <typename T, int MAXT, int MINB>
+static int launch_adj(Context* ctx, const PassParams<T>& p, const AdjArgs<T>& a, int threads) {
+  if (threads < 32 || threads % 32) return set_error(SV_ERR_ARG, "adjoint passes need whole warps");
+  auto kern = k_adjoint_pass<T, MAXT, MINB>;
+  const size_t smem = adjoint_smem<T>(p.kt, threads);
+  static size_t attr = 0;
+  if (smem > attr) {
+    SV_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr"));
+    attr = smem;
+  }
+  int per_sm = 0;
+  SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem), "occupancy"));
+  if (per_sm < 1) return set_error(SV_ERR_ARG, "adjoint tile does not fit on an SM");
+  int64_t grid = (int64_t)per_sm * ctx->num_sms;
+  const int64_t nitems = p.ntiles * a.ncirc;
+  if (grid > nitems) grid = nitems;
+  if (grid > a.gstride) grid = a.gstride;
+  kern<<<(unsigned)grid, threads, smem, ctx->stream>>>(p, a);
+  SV_LAUNCH_CHECK("adjoint pass launch");
+  return SV_OK;
+}
+
+template <typename T>
+static int adjoint_run_typed(Context* ctx, sv_adjoint* A, double h, double* energies, double* grads) {
+  const int n = A->n, nc = A->ncirc;
+  T* const* psi = (T* const*)A->d_ptrs;
+  T* const* lam = psi + nc;
+  const size_t sbytes = A->stride * sizeof(T);
+  cudaStream_t st = ctx->stream;
+  // forward from |0...0>, checkpointing psi after every segment but the last
+  SV_TRY(check_cuda(cudaMemsetAsync(A->d_psi, 0, sbytes * nc, st), "zero"));
+  k_batch_ones<T><<<grid_for(nc, 256), 256, 0, st>>>(psi, nc);
+  SV_LAUNCH_CHECK("ones");
+  const int nseg = (int)A->segs.size();
+  for (int s = 0; s < nseg; s++) {
+    const AdjSegment& sg = A->segs[s];
+    BatchArgs<T> args;
+    memset(&args, 0, sizeof(args));
+    args.states = psi;
+    args.coef = (const T*)sg.d_fcoef;
+    args.coef_stride = (int64_t)sg.fwd->coef_total;
+    args.ncirc = nc;
+    const int threads = 1 << (sg.fwd->kt - kRB);
+    for (const Segment& seg : sg.fwd->segments) {
+      const PassParams<T>& p =
+          *reinterpret_cast<const PassParams<T>*>(sg.fwd->passes.data() + (size_t)seg.pass * sg.fwd->pass_bytes);
+      SV_TRY(launch_pass<T, true>(ctx, p, nullptr, threads, pass_smem<T>(sg.fwd->kt), p.ntiles * nc, st, args));
+    }
+    if (s < nseg - 1)
+      SV_TRY(check_cuda(cudaMemcpyAsync((char*)A->d_cp + (size_t)s * sbytes * nc, A->d_psi, sbytes * nc,
+                                        cudaMemcpyDeviceToDevice, st), "checkpoint"));
+  }
+  // lambda = H psi, energies = Re <psi|lambda>
+  {
+    const int64_t total = ((int64_t)1 << n) * nc;
+    int64_t g = (total + 255) / 256;
+    if (g > (int64_t)ctx->num_sms * 16) g = (int64_t)ctx->num_sms * 16;
+    k_tfim_apply<T><<<(unsigned)g, 256, 0, st>>>(psi, (T* const*)lam, n, nc, h);
+    SV_LAUNCH_CHECK("tfim apply");
+    dim3 grid(A->enb, nc);
+    k_batch_dot_partials<T><<<grid, 256, 0, st>>>(psi, lam, n, A->enb, A->d_epart);
+    SV_LAUNCH_CHECK("energy partials");
+    k_rows_sum<<<grid_for(nc, 128), 128, 0, st>>>(A->d_epart, nc, A->enb, A->d_energy);
+    SV_LAUNCH_CHECK("energy finish");
+  }
+  // reverse sweep
+  SV_TRY(check_cuda(cudaMemsetAsync(A->d_gpart, 0, sizeof(double) * (size_t)nc * A->nparams * A->gstride, st),
+                    "zero gradients"));
+  for (int s = nseg - 1; s >= 0; s--) {
+    if (s < nseg - 1)  // restore the exact forward state at this segment's end
+      SV_TRY(check_cuda(cudaMemcpyAsync(A->d_psi, (char*)A->d_cp + (size_t)s * sbytes * nc, sbytes * nc,
+                                        cudaMemcpyDeviceToDevice, st), "restore"));
+    const AdjSegment& sg = A->segs[s];
+    AdjArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.psi = psi;
+    a.lam = lam;
+    a.coef = (const T*)sg.d_bcoef;
+    a.coef_stride = (int64_t)sg.bwd->coef_total;
+    a.gpart = A->d_gpart;
+    a.ncirc = nc;
+    a.nparams = A->nparams;
+    a.gstride = A->gstride;
+    const int threads = 1 << (sg.bwd->kt - kRB);
+    for (const Segment& seg : sg.bwd->segments) {
+      const PassParams<T>& p =
+          *reinterpret_cast<const PassParams<T>*>(sg.bwd->passes.data() + (size_t)seg.pass * sg.bwd->pass_bytes);
+      if constexpr (sizeof(T) >= 16) SV_TRY(launch_adj<T, 256, 1>(ctx, p, a, threads));
+      else SV_TRY(launch_adj<T, 256, 2>(ctx, p, a, threads));
+    }
+  }
+  k_rows_sum<<<grid_for((int64_t)nc * A->nparams, 128), 128, 0, st>>>(A->d_gpart, (int64_t)nc * A->nparams,
+                                                                      A->gstride, A->d_grad);
+  SV_LAUNCH_CHECK("gradient finish");
+  if (energies)
+    SV_TRY(check_cuda(cudaMemcpyAsync(energies, A->d_energy, nc * sizeof(double), cudaMemcpyDeviceToHost, st), "E"));
+  if (grads)
+    SV_TRY(check_cuda(cudaMemcpyAsync(grads, A->d_grad, (size_t)nc * A->nparams * sizeof(double),
+                                      cudaMemcpyDeviceToHost, st), "grad"));
+  return check_cuda(cudaStreamSynchronize(st), "adjoint sync");
+}
+
+static void adjoint_free(sv_adjoint* A) {
+  if (!A) return;
+  for (auto& s : A->segs) {
+    delete s.fwd;
+    delete s.bwd;
+    if (s.d_fcoef) cudaFree(s.d_fcoef);
+    if (s.d_bcoef) cudaFree(s.d_bcoef);
+  }
+  for (void* p : {A->d_psi, A->d_lam, A->d_cp, A->d_ptrs, (void*)A->d_gpart, (void*)A->d_grad, (void*)A->d_epart,
+                  (void*)A->d_energy})
+    if (p) cudaFree(p);
+  delete A;
+}
+
+}  // namespace sv
+
+extern "C" {
+
+int sv_adjoint_create(sv_context* ctx, int dtype, int ncirc, int nqubits, const sv_gate_op* const* ops, int nops,
+                      const int8_t* generators, const int32_t* params, int nparams, const int32_t* segment_ends,
+                      int nsegments, int tile_bits, sv_adjoint** out) {
+  if (!ctx || !out || !ops || !generators || !params || ncirc < 1 || nops < 1 || nparams < 1 || !segment_ends ||
+      nsegments < 1)
+    return set_error(SV_ERR_ARG, "bad adjoint arguments");
+  *out = nullptr;
+  if (dtype != SV_C128 && dtype != SV_C64) return set_error(SV_ERR_UNSUPPORTED, "adjoint needs a complex dtype");
+  if (nqubits < kRB + 5 || nqubits > 34) return set_error(SV_ERR_ARG, "adjoint needs 9..34 qubits");
+  for (int j = 0; j < nops; j++) {
+    if (generators[j] < 0 || generators[j] > 3) return set_error(SV_ERR_ARG, "op %d: generator must be 0..3", j);
+    if (generators[j] > 0) {
+      if (params[j] < 0 || params[j] >= nparams) return set_error(SV_ERR_ARG, "op %d: parameter out of range", j);
+      if (ops[0][j].ntargets != 1 || ops[0][j].ncontrols != 0)
+        return set_error(SV_ERR_UNSUPPORTED, "op %d: parametrised gates must act on one qubit without controls", j);
+    }
+  }
+  for (int s = 0; s < nsegments; s++)
+    if (segment_ends[s] < 1 || segment_ends[s] > nops || (s > 0 && segment_ends[s] <= segment_ends[s - 1]) ||
+        (s == nsegments - 1 && segment_ends[s] != nops))
+      return set_error(SV_ERR_ARG, "segment ends must increase and end at nops");
+  int kt = 0;
+  // two states per tile: default one bit smaller than a forward tile
+  SV_TRY(check_tile_bits(dtype, nqubits, tile_bits > 0 ? tile_bits : (dtype == SV_C128 ? 10 : 11), &kt));
+  // the reverse sweep reduces with whole-warp shuffles: a tile needs >= 32 threads (2^(kt-4))
+  if (kt < kRB + 5)
+    return set_error(SV_ERR_ARG, "adjoint gradients need tiles of >= %d bits (circuits of >= %d qubits)", kRB + 5,
+                     kRB + 5);
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  sv_adjoint* A = new sv_adjoint();
+  A->dtype = dtype;
+  A->ncirc = ncirc;
+  A->n = nqubits;
+  A->nparams = nparams;
+  A->kt = kt;
+  // parse every circuit (no merging: gradients sit between gates), check one structure
+  for (int c = 0; c < ncirc; c++) {
+    std::vector<HostOp> h;
+    int rc = SV_OK;
+    for (int j = 0; j < nops && rc == SV_OK; j++) {
+      std::vector<HostOp> one;
+      rc = parse_ops(nqubits, &ops[c][j], 1, &one);  // one op: merging cannot apply
+      if (rc == SV_OK) h.push_back(one[0]);
+    }
+    if (rc == SV_OK && c > 0 && !same_structure(A->fops[0], h))
+      rc = set_error(SV_ERR_ARG, "circuit %d differs in structure from circuit 0", c);
+    if (rc != SV_OK) {
+      adjoint_free(A);
+      return rc;
+    }
+    A->fops.push_back(std::move(h));
+  }
+  int rc = SV_OK;
+  int b0 = 0;
+  for (int s = 0; s < nsegments && rc == SV_OK; s++) {
+    const int e0 = segment_ends[s];
+    AdjSegment sg;
+    std::vector<std::vector<HostOp>> fper(ncirc), bper(ncirc);
+    for (int c = 0; c < ncirc; c++) {
+      fper[c].assign(A->fops[c].begin() + b0, A->fops[c].begin() + e0);
+      bper[c] = backward_list(A->fops[c], b0, e0, generators, params);
+    }
+    std::vector<HostOp> f0 = fper[0], bw0 = bper[0];
+    // forward passes hold one state per tile: one bit more than the backward tiles
+    int ktf = kt + 1;
+    if (ktf > nqubits) ktf = nqubits;
+    if (ktf > (dtype == SV_C128 ? 12 : 13)) ktf = kt;
+    rc = plan(dtype, nqubits, ktf, std::move(f0), &sg.fwd);
+    if (rc == SV_OK) rc = plan(dtype, nqubits, kt, std::move(bw0), &sg.bwd);
+    if (rc == SV_OK && (sg.fwd->nunfused || sg.bwd->nunfused))
+      rc = set_error(SV_ERR_UNSUPPORTED, "adjoint circuits need gates on at most 2 targets");
+    if (rc == SV_OK)
+      rc = dtype == SV_C128 ? gather_coef<c128>(sg.fwd, fper, &sg.d_fcoef) : gather_coef<c64>(sg.fwd, fper, &sg.d_fcoef);
+    if (rc == SV_OK)
+      rc = dtype == SV_C128 ? gather_coef<c128>(sg.bwd, bper, &sg.d_bcoef) : gather_coef<c64>(sg.bwd, bper, &sg.d_bcoef);
+    A->segs.push_back(sg);
+    b0 = e0;
+  }
+  const size_t es = dtype_size(dtype);
+  A->stride = ((((size_t)1 << nqubits) * es + 255) / 256) * 256 / es;
+  const size_t sbytes = A->stride * es;
+  A->gstride = ctx->num_sms * 4;
+  A->enb = 64;
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_psi, sbytes * ncirc), "psi");
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_lam, sbytes * ncirc), "lambda");
+  if (rc == SV_OK && nsegments > 1)
+    rc = check_cuda(cudaMalloc(&A->d_cp, sbytes * ncirc * (nsegments - 1)), "checkpoints");
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_gpart, sizeof(double) * (size_t)ncirc * nparams * A->gstride), "g");
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_grad, sizeof(double) * (size_t)ncirc * nparams), "grad");
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_epart, sizeof(double) * (size_t)ncirc * A->enb), "e");
+  if (rc == SV_OK) rc = check_cuda(cudaMalloc(&A->d_energy, sizeof(double) * ncirc), "energy");
+  if (rc == SV_OK) {
+    std::vector<void*> ptrs(2 * ncirc);
+    for (int c = 0; c < ncirc; c++) {
+      ptrs[c] = (char*)A->d_psi + c * sbytes;
+      ptrs[ncirc + c] = (char*)A->d_lam + c * sbytes;
+    }
+    rc = check_cuda(cudaMalloc(&A->d_ptrs, ptrs.size() * sizeof(void*)), "pointers");
+    if (rc == SV_OK)
+      rc = check_cuda(cudaMemcpy(A->d_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice), "ptrs");
+  }
+  if (rc != SV_OK) {
+    adjoint_free(A);
+    return rc;
+  }
+  *out = A;
+  return SV_OK;
+}
+
+int sv_adjoint_update(sv_context* ctx, sv_adjoint* A, const sv_gate_op* const* ops, int nops,
+                      const int8_t* generators, const int32_t* params) {
+  if (!ctx || !A || !ops || !generators || !params) return set_error(SV_ERR_ARG, "bad adjoint update");
+  if (nops != (int)A->fops[0].size()) return set_error(SV_ERR_ARG, "op count differs from the planned circuits");
+  for (int c = 0; c < A->ncirc; c++) {
+    std::vector<HostOp> h;
+    for (int j = 0; j < nops; j++) {
+      std::vector<HostOp> one;
+      SV_TRY(parse_ops(A->n, &ops[c][j], 1, &one));
+      h.push_back(one[0]);
+    }
+    if (!same_structure(A->fops[0], h)) return set_error(SV_ERR_ARG, "circuit %d changed structure", c);
+    A->fops[c] = std::move(h);
+  }
+  int b0 = 0;
+  for (auto& sg : A->segs) {
+    const int e0 = b0 + (int)sg.fwd->ops.size();
+    std::vector<std::vector<HostOp>> fper(A->ncirc), bper(A->ncirc);
+    for (int c = 0; c < A->ncirc; c++) {
+      fper[c].assign(A->fops[c].begin() + b0, A->fops[c].begin() + e0);
+      bper[c] = backward_list(A->fops[c], b0, e0, generators, params);
+    }
+    if (A->dtype == SV_C128) {
+      SV_TRY(gather_coef<c128>(sg.fwd, fper, &sg.d_fcoef));
+      SV_TRY(gather_coef<c128>(sg.bwd, bper, &sg.d_bcoef));
+    } else {
+      SV_TRY(gather_coef<c64>(sg.fwd, fper, &sg.d_fcoef));
+      SV_TRY(gather_coef<c64>(sg.bwd, bper, &sg.d_bcoef));
+    }
+    b0 = e0;
+  }
+  return SV_OK;
+}
+
+int sv_adjoint_run(sv_context* ctx, sv_adjoint* A, double h, double* energies, double* grads) {
+  if (!ctx || !A) return set_error(SV_ERR_ARG, "null context or adjoint");
+  return A->dtype == SV_C128 ? adjoint_run_typed<c128>(ctx, A, h, energies, grads)
+                             : adjoint_run_typed<c64>(ctx, A, h, energies, grads);
+}
+
+int sv_adjoint_state(const sv_adjoint* A, int circuit, void** psi) {
+  if (!A || circuit < 0 || circuit >= A->ncirc || !psi) return set_error(SV_ERR_ARG, "bad adjoint query");
+  *psi = (char*)A->d_psi + (size_t)circuit * A->stride * dtype_size(A->dtype);
+  return SV_OK;
+}
+
+int sv_adjoint_destroy(sv_adjoint* A) {
+  adjoint_free(A);
   return SV_OK;
 }
 

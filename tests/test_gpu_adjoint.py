@@ -1,0 +1,121 @@
+"""Adjoint gradients against parameter shift on the CPU oracle (the reference's kernels
+restated), central finite differences in complex128, and complex64 vs complex128."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from qibojit_gb300.batch import tfim_energy_dense
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def backend():
+    from qibojit_gb300 import MetaBackend
+
+    return MetaBackend.load("gb300")
+
+
+def oracle_energy(n, layers, p, h=1.0):
+    """HEA forward on the CPU oracle kernels, TFIM energy in numpy."""
+    ob = O.OracleBackend()
+    s = ob.zero_state(n)
+    for layer in range(layers):
+        for q in range(n):
+            t, f = p[layer, q]
+            ry = np.array([[np.cos(t / 2), -np.sin(t / 2)], [np.sin(t / 2), np.cos(t / 2)]], dtype=complex)
+            rz = np.diag([np.exp(-0.5j * f), np.exp(0.5j * f)])
+            s = ob._one_qubit_base(s, n, q, "apply_gate", ry, ob.qubits_tensor(n, [q]))
+            s = ob._one_qubit_base(s, n, q, "apply_gate", rz, ob.qubits_tensor(n, [q]))
+        for q in range(n - 1):
+            s = ob._one_qubit_base(s, n, q + 1, "apply_x", None, ob.qubits_tensor(n, [q + 1], [q]))
+    return tfim_energy_dense(s, n, h), s
+
+
+def test_adjoint_matches_parameter_shift(backend):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    n, L, nc = 9, 3, 2
+    rng = np.random.default_rng(11)
+    params = rng.uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    eng = AdjointTFIM(backend, n, L, nc, "complex128", h=1.0, checkpoint_every=2)
+    E, G = eng(params)
+    for c in range(nc):
+        e0, _ = oracle_energy(n, L, params[c])
+        assert abs(E[c] - e0) < 1e-11
+        for (layer, q, k) in [(0, 0, 0), (0, 8, 1), (1, 3, 0), (2, 5, 1), (2, 0, 0), (1, 6, 1)]:
+            pp, pm = params[c].copy(), params[c].copy()
+            pp[layer, q, k] += np.pi / 2
+            pm[layer, q, k] -= np.pi / 2
+            shift = (oracle_energy(n, L, pp)[0] - oracle_energy(n, L, pm)[0]) / 2
+            assert abs(G[c, layer, q, k] - shift) < 1e-10, (c, layer, q, k, G[c, layer, q, k], shift)
+
+
+def test_adjoint_matches_finite_differences(backend):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    n, L = 9, 2
+    rng = np.random.default_rng(12)
+    p = rng.uniform(0, 2 * np.pi, size=(1, L, n, 2))
+    eng = AdjointTFIM(backend, n, L, 1, "complex128", checkpoint_every=1)
+    E, G = eng(p)
+    fd = np.zeros_like(p)
+    step = 1e-4
+    probe = AdjointTFIM(backend, n, L, 1, "complex128", checkpoint_every=1)
+    for idx in np.ndindex(p.shape):
+        a, b = p.copy(), p.copy()
+        a[idx] += step
+        b[idx] -= step
+        fd[idx] = (probe(a)[0][0] - probe(b)[0][0]) / (2 * step)
+    np.testing.assert_allclose(G, fd, atol=1e-7)
+
+
+@pytest.mark.parametrize("every", [1, 2, 10])
+def test_checkpointing_does_not_change_results(backend, every):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    n, L, nc = 10, 4, 3
+    p = np.random.default_rng(13).uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    E1, G1 = AdjointTFIM(backend, n, L, nc, "complex128", checkpoint_every=every)(p)
+    E2, G2 = AdjointTFIM(backend, n, L, nc, "complex128", checkpoint_every=L)(p)
+    np.testing.assert_allclose(E1, E2, atol=1e-12)
+    np.testing.assert_allclose(G1, G2, atol=1e-11)
+
+
+def test_complex64_gradients_track_complex128(backend):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    n, L, nc = 12, 5, 4
+    p = np.random.default_rng(14).uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    E64, G64 = AdjointTFIM(backend, n, L, nc, "complex64", checkpoint_every=2)(p)
+    E128, G128 = AdjointTFIM(backend, n, L, nc, "complex128", checkpoint_every=2)(p)
+    np.testing.assert_allclose(E64, E128, atol=2e-5)
+    np.testing.assert_allclose(G64, G128, atol=2e-4)
+
+
+def test_small_circuits_are_rejected(backend):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    with pytest.raises(ValueError):
+        AdjointTFIM(backend, 8, 2, 1, "complex128")(np.zeros((1, 2, 8, 2)))
+
+
+def test_update_and_autograd(backend):
+    import torch
+
+    from qibojit_gb300.adjoint import AdjointTFIM, HEAEnergy
+
+    n, L, nc = 9, 2, 2
+    rng = np.random.default_rng(15)
+    eng = AdjointTFIM(backend, n, L, nc, "complex128")
+    p1 = rng.uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    p2 = rng.uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    eng(p1)
+    E2, G2 = eng(p2)  # re-uses plans and memory
+    E2b, G2b = AdjointTFIM(backend, n, L, nc, "complex128")(p2)
+    np.testing.assert_allclose(E2, E2b, atol=1e-13)
+    np.testing.assert_allclose(G2, G2b, atol=1e-13)
+    t = torch.tensor(p2, dtype=torch.float64, requires_grad=True)
+    loss = HEAEnergy.apply(t, eng).sum()
+    loss.backward()
+    np.testing.assert_allclose(t.grad.numpy(), G2, atol=1e-13)
