@@ -289,6 +289,7 @@ def run_engine(args):
         }
         del s128, s64
         torch.cuda.empty_cache()
+        variants.update(_extra_workloads(torch, backend, stream, args))
 
     peak, peak_kind = _peak_hbm()
     pass_bytes = 2 * itemsize * (1 << n)
@@ -322,6 +323,130 @@ def run_engine(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _extra_workloads(torch, backend, stream, args):
+    """The other configurations of the same engine, one bounded measurement each:
+    QFT n=20 complex128 (parity against sqrt(N) * ifft), the batched VQE forward pass
+    (4096 hardware-efficient-ansatz circuits, n ~ U{10..22}, L ~ U{4..12}, TFIM
+    energies) and adjoint TFIM gradients (n=26, 20 layers, 1040 parameters)."""
+    from oracle import pyoracle as O
+    from qibojit_gb300 import circuits
+    from qibojit_gb300.adjoint import AdjointTFIM
+    from qibojit_gb300.batch import BatchedCircuits, hea_batch
+
+    out = {}
+    # ---- QFT n=20, complex128
+    n = 20
+    q = circuits.qft(n)
+    x = np.random.default_rng(SEED).standard_normal(2**n) + 1j * np.random.default_rng(SEED + 1).standard_normal(2**n)
+    x /= np.linalg.norm(x)
+    xd = backend.cast(x)
+    res = {}
+    for mode in ("plain", "fused"):
+        s = backend.execute_circuit(q, xd, fuse=(mode == "fused"))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            s = backend.execute_circuit(q, xd, fuse=(mode == "fused"))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[f"qft_n20_c128_{mode}_gates_per_s"] = len(q.queue) * 5 / (e0.elapsed_time(e1) / 1000.0)
+        res[f"qft_n20_c128_{mode}_max_abs_err_vs_ifft"] = float(
+            np.abs(backend.to_numpy(s) - np.sqrt(2**n) * np.fft.ifft(x)).max())
+    ob = O.OracleBackend()
+    ref = x.copy()
+    cm = backend.custom_matrices
+    t0 = time.perf_counter()
+    for g in q.queue:
+        qt = ob.qubits_tensor(n, g.target_qubits, g.control_qubits)
+        name = type(g).__name__
+        if name == "H":
+            ob._one_qubit_base(ref, n, g.target_qubits[0], "apply_gate", cm.H, qt)
+        elif name == "CU1":
+            ob._one_qubit_base(ref, n, g.target_qubits[0], "apply_z_pow", cm.CU1(*g.parameters), qt)
+        else:
+            ob._two_qubit_base(ref, n, *g.target_qubits, "apply_swap", None, qt)
+    res["qft_n20_c128_cpu_reference_gates_per_s"] = len(q.queue) / (time.perf_counter() - t0)
+    out["qft"] = res
+    # ---- batched VQE forward, 4096 circuits
+    specs = hea_batch(4096, seed=SEED)
+    vq = {}
+    for dt, reps in (("complex64", 3), ("complex128", 1)):
+        t0 = time.perf_counter()
+        bat = BatchedCircuits.from_hea(backend, specs, dt)
+        create_s = time.perf_counter() - t0
+        bat.run()  # eager run + CUDA graph capture
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            bat.run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        t0 = time.perf_counter()
+        en = bat.tfim_energies(1.0)
+        vq[dt] = {"circuits_per_s": 4096 / (ms / 1000.0), "ms_per_batch": ms, "energy_ms":
+                  1000 * (time.perf_counter() - t0), "plan_s": create_s, "stats": bat.stats()}
+        vq[dt]["energies_head"] = [float(v) for v in en[:3]]
+        if dt == "complex64":
+            e64 = en.copy()
+        else:
+            vq["max_abs_energy_diff_c64_vs_c128"] = float(np.abs(e64 - en).max())
+        bat.close()
+        del bat
+        torch.cuda.empty_cache()
+    # CPU baseline on a sample: the oracle's per-gate kernels on the first 8 circuits
+    from qibojit_gb300.batch import hea_circuit
+
+    t0 = time.perf_counter()
+    ngates = 0
+    for nq, L, prm in specs[:8]:
+        c = hea_circuit(nq, L, prm)
+        st = ob.zero_state(nq, "complex64")
+        for g in c.queue:
+            qt = ob.qubits_tensor(nq, g.target_qubits, g.control_qubits)
+            name = type(g).__name__
+            if name == "CNOT":
+                ob._one_qubit_base(st, nq, g.target_qubits[0], "apply_x", None, qt)
+            else:
+                ob._one_qubit_base(st, nq, g.target_qubits[0], "apply_gate", g.base_matrix("complex64"), qt)
+            ngates += 1
+    vq["cpu_reference_sample"] = {"circuits_per_s": 8 / (time.perf_counter() - t0),
+                                  "sample": "first 8 circuits, per-gate C/OpenMP restatement, complex64"}
+    out["vqe_forward_4096"] = vq
+    # ---- adjoint gradients: one wave of 64 circuits, n=26, 20 layers, complex64
+    nq, L, wave = 26, 20, 64
+    prm = np.random.default_rng(SEED).uniform(0, 2 * np.pi, size=(wave, L, nq, 2))
+    eng = AdjointTFIM(backend, nq, L, wave, "complex64", checkpoint_every=5)
+    eng(prm)  # plans and allocates
+    t0 = time.perf_counter()
+    E, G = eng(prm)
+    dt_s = time.perf_counter() - t0
+    eng.close()
+    del eng
+    torch.cuda.empty_cache()
+    # CPU: one forward evaluation of two layers on the oracle, scaled to a parameter-shift gradient
+    c = hea_circuit(nq, 2, prm[0, :2])
+    st = ob.zero_state(nq, "complex64")
+    t0 = time.perf_counter()
+    for g in c.queue:
+        qt = ob.qubits_tensor(nq, g.target_qubits, g.control_qubits)
+        if type(g).__name__ == "CNOT":
+            ob._one_qubit_base(st, nq, g.target_qubits[0], "apply_x", None, qt)
+        else:
+            ob._one_qubit_base(st, nq, g.target_qubits[0], "apply_gate", g.base_matrix("complex64"), qt)
+    t_two = time.perf_counter() - t0
+    del st
+    t_eval = t_two * L / 2
+    out["adjoint_n26_L20"] = {"gradient_vectors_per_s": wave / dt_s, "wave": wave, "params_per_circuit": 2 * L * nq,
+                              "s_per_wave": dt_s, "energy_head": [float(v) for v in E[:2]],
+                              "cpu_parameter_shift_gradient_vectors_per_s_estimate": 1.0 / (2 * 2 * L * nq * t_eval),
+                              "cpu_sample": f"2 of {L} layers forward on the oracle ({t_two:.1f} s), scaled to "
+                                            f"{2 * 2 * L * nq} shifted evaluations"}
+    return out
 
 
 def main():

@@ -86,6 +86,57 @@ class BatchedCircuits:
         self._h = h
         self.nqubits = [c.nqubits for c in circuits]
 
+    @classmethod
+    def from_hea(cls, backend, specs, dtype: str = "complex64", tile_bits: int = 0):
+        """Batch of hardware-efficient-ansatz circuits from ``hea_batch`` specs, with the
+        op arrays built directly from the angles (no per-gate Python objects)."""
+        self = cls.__new__(cls)
+        self.backend, self.ctx, self.lib, self.dtype = backend, backend.ctx, backend.lib, dtype
+        self.ncirc = len(specs)
+        self.nqubits = [n for n, _, _ in specs]
+        nq = (ctypes.c_int32 * self.ncirc)(*self.nqubits)
+        ptrs = (ctypes.c_void_p * self.ncirc)()
+        counts = (ctypes.c_int32 * self.ncirc)()
+        x = np.array([0.0, 0.0, 1.0, 0.0, 1.0, 0.0, 0.0, 0.0])
+        keep = [x]
+        for i, (n, layers, params) in enumerate(specs):
+            th = params[..., 0].reshape(-1) / 2
+            ph = params[..., 1].reshape(-1) / 2
+            c, s_ = np.cos(th), np.sin(th)
+            z = np.zeros_like(c)
+            ry = np.ascontiguousarray(np.stack([c, z, -s_, z, s_, z, c, z], axis=-1))
+            rz = np.ascontiguousarray(np.stack([np.cos(ph), -np.sin(ph), np.cos(ph), np.sin(ph)], axis=-1))
+            keep += [ry, rz]
+            nops = layers * (3 * n - 1)
+            arr = (GateOp * nops)()
+            k = 0
+            for layer in range(layers):
+                for q in range(n):
+                    a = arr[k]
+                    a.kind, a.ntargets = 0, 1
+                    a.targets[0] = q
+                    a.matrix = ry[layer * n + q].ctypes.data
+                    b = arr[k + 1]
+                    b.kind, b.ntargets = 1, 1
+                    b.targets[0] = q
+                    b.matrix = rz[layer * n + q].ctypes.data
+                    k += 2
+                for q in range(n - 1):
+                    a = arr[k]
+                    a.kind, a.ntargets, a.ncontrols = 0, 1, 1
+                    a.targets[0] = q + 1
+                    a.controls[0] = q
+                    a.matrix = x.ctypes.data
+                    k += 1
+            keep.append(arr)
+            ptrs[i] = ctypes.cast(arr, ctypes.c_void_p).value
+            counts[i] = nops
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.sv_batch_create(self.ctx.handle, _lib.DTYPE_CODES[dtype], self.ncirc, nq, ptrs, counts,
+                                            int(tile_bits), ctypes.byref(h)), "sv_batch_create")
+        self._h = h
+        return self
+
     def stats(self) -> dict:
         g, p, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
         _lib.check(self.lib.sv_batch_stats(self._h, ctypes.byref(g), ctypes.byref(p), ctypes.byref(b)))

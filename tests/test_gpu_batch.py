@@ -33,6 +33,15 @@ def test_hea_batch_matches_single_circuits(backend, dt, tol):
         assert abs(energies[i] - e) < (1e-11 if dtype == "complex128" else 1e-4) * max(1.0, abs(e))
 
 
+def test_from_hea_matches_gate_objects(backend):
+    specs = hea_batch(12, seed=21, nmin=9, nmax=13, lmin=2, lmax=4)
+    a = BatchedCircuits(backend, [hea_circuit(n, L, p) for n, L, p in specs], "complex128")
+    b = BatchedCircuits.from_hea(backend, specs, "complex128")
+    a.run()
+    b.run()
+    np.testing.assert_allclose(a.tfim_energies(), b.tfim_energies(), atol=1e-13)
+
+
 def test_batch_graph_replay_is_repeatable(backend):
     specs = hea_batch(64, seed=9, nmin=8, nmax=16, lmin=2, lmax=6)
     batch = BatchedCircuits(backend, [hea_circuit(n, L, p) for n, L, p in specs], "complex64")
