@@ -179,6 +179,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def replicas_throughput(elapsed_ms: float, units_per_rank: float, device: str = "cuda"):
+    """Whole-job throughput of N independent replicas (one circuit per rank, no data
+    exchange): the units of all ranks over the slowest rank's time.  Returns
+    (max elapsed ms, units/s)."""
+    import torch
+
+    dist = torch.distributed
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    if ws > 1:
+        t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    return elapsed_ms, ws * units_per_rank / (elapsed_ms / 1000.0)
+
+
 def _time_program(torch, prog, backend, state, dcode, n, steps, stream):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -228,13 +243,9 @@ def run_engine(args):
     zs_ms = _time_program(torch, type("Z", (), {"run": staticmethod(lambda s: s)}), backend, state, dcode, n, 3, stream)
     with ClockSampler(dev) as clocks:
         ms_step = _time_program(torch, prog, backend, state, dcode, n, args.steps, stream)
-    elapsed_ms = ms_step * args.steps
+    elapsed_ms, value = replicas_throughput(elapsed_ms, ngates * args.steps, "cuda")
     if ws > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
         torch.distributed.barrier()
-    value = ws * ngates * args.steps / (elapsed_ms / 1000.0)
     pass_ms = (ms_step - zs_ms) / st["passes"]
 
     # ---- end to end through the public API: pinned host -> device -> host every step

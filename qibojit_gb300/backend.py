@@ -166,20 +166,61 @@ class GB300Backend(_QiboBackend):
 
     # -------------------------------------------------------------- state creation
     def zero_state(self, nqubits: int, density_matrix: bool = False, dtype=None):
-        if density_matrix:
-            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+        """|0...0> (or |0><0| as a 2^n x 2^n matrix, cpu.py:334-353)."""
         dtype = _dtype_name(dtype) if dtype is not None else self.dtype
         torch = _torch()
-        state = torch.empty(1 << nqubits, dtype=_torch_dtype(dtype), device=self._tdevice)
-        _lib.check(self.lib.sv_zero_state(self.ctx.handle, state.data_ptr(), _lib.DTYPE_CODES[dtype], int(nqubits)),
+        nbits = 2 * nqubits if density_matrix else nqubits
+        state = torch.empty(1 << nbits, dtype=_torch_dtype(dtype), device=self._tdevice)
+        _lib.check(self.lib.sv_zero_state(self.ctx.handle, state.data_ptr(), _lib.DTYPE_CODES[dtype], int(nbits)),
                    "zero_state")
-        return state
+        return state.reshape(1 << nqubits, 1 << nqubits) if density_matrix else state
 
     # ------------------------------------------------------------- gate dispatch
     def apply_gate(self, gate, state, nqubits: int, inverse: bool = False):
         if len(tuple(state.shape)) == 2:
-            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
+            return self._apply_gate_density_matrix(gate, state, nqubits, inverse)
         return self._apply_gate(gate, state, nqubits)
+
+    def _apply_gate_density_matrix(self, gate, state, nqubits: int, inverse: bool = False):
+        """rho -> U rho U^dagger as two calls on the 2n-qubit vector (cpu.py:452-498): U
+        on the row qubits (bits shifted up by n), conj(U) on the column qubits."""
+        name = type(gate).__name__
+        dtype = _dtype_name(state.dtype)
+        if inverse:
+            u = np.linalg.inv(np.asarray(gate.matrix(self)))
+            matrix = u if len(gate.control_qubits) == 0 else None
+            if matrix is None:
+                raise NotImplementedError("inverse of a controlled gate on a density matrix")
+            gate = type("Inverse", (), {"target_qubits": gate.target_qubits, "control_qubits": (),
+                                         "parameters": (), "name": "inverse"})()
+            name = "Unitary"
+        else:
+            matrix = self._as_custom_matrix(gate, dtype)
+        qubits = self._create_qubits_tensor(gate, nqubits)
+        qubits_dm = qubits + nqubits
+        targets = gate.target_qubits
+        targets_dm = tuple(q + nqubits for q in targets)
+        shape = state.shape
+        flat = state.reshape(-1)
+        if not flat.is_contiguous():
+            flat = flat.contiguous()
+        n2 = 2 * nqubits
+        if name in ("Y", "CY"):
+            flat = self._one_qubit_base(flat, n2, *targets, "apply_y", matrix, qubits_dm)
+            flat = self._one_qubit_base(flat, n2, *targets_dm, "apply_gate", np.conj(self.custom_matrices.Y),
+                                        qubits)
+        elif len(targets) == 1:
+            op = GATE_OPS.get(name, "apply_gate")
+            flat = self._one_qubit_base(flat, n2, *targets, op, matrix, qubits_dm)
+            flat = self._one_qubit_base(flat, n2, *targets_dm, op, np.conj(matrix), qubits)
+        elif len(targets) == 2:
+            op = GATE_OPS.get(name, "apply_two_qubit_gate")
+            flat = self._two_qubit_base(flat, n2, *targets, op, matrix, qubits_dm)
+            flat = self._two_qubit_base(flat, n2, *targets_dm, op, np.conj(matrix), qubits)
+        else:
+            flat = self._multi_qubit_base(flat, n2, targets, matrix, qubits_dm)
+            flat = self._multi_qubit_base(flat, n2, targets_dm, np.conj(matrix), qubits)
+        return flat.reshape(shape)
 
     def _create_qubits_tensor(self, gate, nqubits: int):
         qubits = [nqubits - q - 1 for q in gate.control_qubits]
@@ -361,6 +402,10 @@ class GB300Backend(_QiboBackend):
                               copy=True)
         dtype = _dtype_name(state.dtype)
         fuse = self.fusion if fuse is None else fuse
+        if state.dim() == 2:  # density matrix: gate by gate, U on rows and conj(U) on columns
+            for gate in circuit.queue:
+                state = self.apply_gate(gate, state, n)
+            return state
         if fuse and n >= 8 and dtype in ("complex128", "complex64") and circuit.queue:
             key = (id(circuit), len(circuit.queue), n, dtype)
             prog = self._programs.get(key)

@@ -154,7 +154,7 @@ NONZERO.extend(itertools.combinations(range(8), r=4))
 NSHOTS = (len(NONZERO) // 2 + 1) * [1000, 200000]
 
 
-@pytest.mark.parametrize("nonzero,nshots", zip(NONZERO, NSHOTS))
+@pytest.mark.parametrize("nonzero,nshots", list(zip(NONZERO, NSHOTS)))
 def test_measure_frequencies_sparse_probabilities(backend, nonzero, nshots):
     probs = np.zeros(8, dtype=np.float64)
     for i in nonzero:
