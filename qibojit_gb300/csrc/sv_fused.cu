@@ -1670,6 +1670,16 @@ __global__ void __launch_bounds__(MAXT, MINB) k_adjoint_pass(const __grid_consta
           if (lane == 0) gacc[op.u1 * nwarps + warp] += (double)acc;
           continue;
         }
+        if (type == FOP_D1RUN) {
+          // uncontrolled complex 2x2 gates on distinct register bits (fixed gates of the circuit)
+          const T* c = cbase + op.coef;
+#pragma unroll 1
+          for (int k = 0; k < op.nrun; k++) {
+            dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+            dense1_dispatch(w, c + 4 * k, op.ru[k], 0xffffu);
+          }
+          continue;
+        }
         const int flags = op.flags;
         if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
         if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;

@@ -119,3 +119,99 @@ def test_update_and_autograd(backend):
     loss = HEAEnergy.apply(t, eng).sum()
     loss.backward()
     np.testing.assert_allclose(t.grad.numpy(), G2, atol=1e-13)
+
+
+def _random_unitary(rng):
+    q, r = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+@pytest.mark.parametrize("dt", ["complex128", "complex64"])
+def test_fixed_complex_gates_inside_adjoint_circuits(backend, dt):
+    """A layer of parameter-free complex one-qubit gates (the planner fuses consecutive
+    ones into register runs) before every RY/RZ layer: energies and gradients against
+    the CPU oracle and parameter shift."""
+    import ctypes
+
+    from qibojit_gb300 import _lib
+    from qibojit_gb300.fusion import GateOp
+
+    n, L = 9, 2
+    rng = np.random.default_rng(16)
+    fixed = [[_random_unitary(rng) for _ in range(n)] for _ in range(L)]
+    theta = rng.uniform(0, 2 * np.pi, size=(L, n, 2))
+    keep = []
+
+    def mat(m):
+        buf = np.ascontiguousarray(np.column_stack([m.real.ravel(), m.imag.ravel()]).ravel(), dtype=np.float64)
+        keep.append(buf)
+        return buf.ctypes.data
+
+    def circuit_ops(p):
+        ops, gens, pidx = [], [], []
+        for layer in range(L):
+            for q in range(n):
+                ops.append((0, q, -1, mat(fixed[layer][q])))
+                gens.append(0)
+                pidx.append(-1)
+            for q in range(n):
+                t, f = p[layer, q]
+                ops.append((0, q, -1, mat(np.array([[np.cos(t / 2), -np.sin(t / 2)], [np.sin(t / 2), np.cos(t / 2)]]))))
+                gens.append(2)
+                pidx.append((layer * n + q) * 2)
+                ops.append((1, q, -1, mat(np.array([np.exp(-0.5j * f), np.exp(0.5j * f)]))))
+                gens.append(3)
+                pidx.append((layer * n + q) * 2 + 1)
+            for q in range(n - 1):
+                ops.append((0, q + 1, q, mat(np.array([[0, 1], [1, 0]], dtype=complex))))
+                gens.append(0)
+                pidx.append(-1)
+        arr = (GateOp * len(ops))()
+        for k, (kind, t, c, m) in enumerate(ops):
+            arr[k].kind, arr[k].ntargets = kind, 1
+            arr[k].targets[0] = t
+            if c >= 0:
+                arr[k].ncontrols = 1
+                arr[k].controls[0] = c
+            arr[k].matrix = m
+        return arr, np.array(gens, dtype=np.int8), np.array(pidx, dtype=np.int32)
+
+    def oracle_energy(p):
+        ob = O.OracleBackend()
+        s = ob.zero_state(n)
+        for layer in range(L):
+            for q in range(n):
+                s = ob._one_qubit_base(s, n, q, "apply_gate", fixed[layer][q], ob.qubits_tensor(n, [q]))
+            for q in range(n):
+                t, f = p[layer, q]
+                ry = np.array([[np.cos(t / 2), -np.sin(t / 2)], [np.sin(t / 2), np.cos(t / 2)]], dtype=complex)
+                rz = np.diag([np.exp(-0.5j * f), np.exp(0.5j * f)])
+                s = ob._one_qubit_base(s, n, q, "apply_gate", ry, ob.qubits_tensor(n, [q]))
+                s = ob._one_qubit_base(s, n, q, "apply_gate", rz, ob.qubits_tensor(n, [q]))
+            for q in range(n - 1):
+                s = ob._one_qubit_base(s, n, q + 1, "apply_x", None, ob.qubits_tensor(n, [q + 1], [q]))
+        return tfim_energy_dense(s, n, 1.0)
+
+    arr, gens, pidx = circuit_ops(theta)
+    nops, nparams = len(gens), L * n * 2
+    ptrs = (ctypes.c_void_p * 1)(ctypes.cast(arr, ctypes.c_void_p).value)
+    per_layer = 4 * n - 1
+    ends = np.array([per_layer, nops], dtype=np.int32)
+    lib, h = backend.lib, ctypes.c_void_p()
+    _lib.check(lib.sv_adjoint_create(backend.ctx.handle, _lib.DTYPE_CODES[dt], 1, n, ptrs, nops, gens.ctypes.data,
+                                     pidx.ctypes.data, nparams, ends.ctypes.data, len(ends), 0, ctypes.byref(h)))
+    try:
+        E = np.zeros(1)
+        G = np.zeros((1, nparams))
+        _lib.check(lib.sv_adjoint_run(backend.ctx.handle, h, 1.0, E.ctypes.data, G.ctypes.data))
+    finally:
+        lib.sv_adjoint_destroy(h)
+    tol_e, tol_g = (1e-11, 1e-10) if dt == "complex128" else (2e-5, 2e-4)
+    assert abs(E[0] - oracle_energy(theta)) < tol_e
+    G = G.reshape(L, n, 2)
+    for (layer, q, k) in [(0, 0, 0), (0, 4, 1), (1, 8, 0), (1, 2, 1)]:
+        pp, pm = theta.copy(), theta.copy()
+        pp[layer, q, k] += np.pi / 2
+        pm[layer, q, k] -= np.pi / 2
+        shift = (oracle_energy(pp) - oracle_energy(pm)) / 2
+        assert abs(G[layer, q, k] - shift) < tol_g, (layer, q, k, G[layer, q, k], shift)
