@@ -485,6 +485,74 @@ static int coef_cost(const HostOp& h) {
 // Builds the phase-local form of the scheduled ops of one pass.
 // Every coefficient slot of a pass records where it came from (op index, entry), so a
 // circuit with the same structure and other parameters can refill the slots.
+// Consecutive sign diagonals of one phase commute and act as one: merge each run of
+// them (without thread or tile controls) into a single FOP_SIGN whose negate table is
+// indexed by the union of their non-register bits, while that union has <= 3 bits.
+static void merge_signs(FOp* ops, int begin, int* end) {
+  auto descs = [](const FOp& f, int (*d)[2], int* slot) {  // non-register bits and their table slots
+    int k = 0;
+    for (int i = 0; i < f.nd; i++) {
+      if (f.tb[i] < 0 && f.ob[i] < 0) continue;
+      d[k][0] = f.tb[i];
+      d[k][1] = f.ob[i];
+      slot[k] = f.nd - 1 - i;
+      k++;
+    }
+    return k;
+  };
+  int w = begin;
+  for (int r = begin; r < *end; r++) {
+    FOp f = ops[r];
+    const bool plain_sign = f.type == FOP_SIGN && f.omask == 0 && f.tmask == 0;
+    if (plain_sign && w > begin) {
+      FOp& g = ops[w - 1];
+      if (g.type == FOP_SIGN && g.omask == 0 && g.tmask == 0) {
+        int dg[3][2], sg[3], df[3][2], sf[3];
+        const int ng = descs(g, dg, sg), nf = descs(f, df, sf);
+        int du[3][2], nu = 0, mapg[3], mapf[3];
+        bool fits = true;
+        for (int a = 0; a < ng + nf && fits; a++) {
+          const int* d = a < ng ? dg[a] : df[a - ng];
+          int u = 0;
+          while (u < nu && !(du[u][0] == d[0] && du[u][1] == d[1])) u++;
+          if (u == nu) {
+            if (nu == 3) {
+              fits = false;
+              break;
+            }
+            du[nu][0] = d[0];
+            du[nu][1] = d[1];
+            nu++;
+          }
+          (a < ng ? mapg[a] : mapf[a - ng]) = u;
+        }
+        if (fits) {
+          FOp m;
+          memset(&m, 0, sizeof(m));
+          m.type = FOP_SIGN;
+          m.nd = (uint8_t)nu;
+          m.jmask = 0xffffu;
+          for (int i = 0; i < 3; i++) {
+            m.tb[i] = i < nu ? (int8_t)du[i][0] : (int8_t)-1;
+            m.ob[i] = i < nu ? (int8_t)du[i][1] : (int8_t)-1;
+          }
+          // union entry u sits at table bit nu - 1 - u
+          for (int t = 0; t < (1 << nu); t++) {
+            int tg = 0, tf = 0;
+            for (int a = 0; a < ng; a++) tg |= ((t >> (nu - 1 - mapg[a])) & 1) << sg[a];
+            for (int a = 0; a < nf; a++) tf |= ((t >> (nu - 1 - mapf[a])) & 1) << sf[a];
+            m.neg[t] = (uint16_t)(g.neg[tg] ^ f.neg[tf]);
+          }
+          g = m;
+          continue;
+        }
+      }
+    }
+    ops[w++] = f;
+  }
+  *end = w;
+}
+
 template <typename T>
 static void encode_pass(const sv_program* prog, const std::vector<int>& sched, uint64_t S, PassParams<T>* pp,
                         int* nphases_out, std::vector<int32_t>* src) {
@@ -657,6 +725,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         }
       }
     }
+    merge_signs(pp->ops, P.op_begin, &nops);
     // merge runs of uncontrolled one-target dense ops into FOP_D1RUN records
     {
       int w = P.op_begin;
