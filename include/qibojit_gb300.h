@@ -205,6 +205,15 @@ int sv_program_run(sv_context* ctx, const sv_program* prog, void* state);
 int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* nfused_gates,
                      int* tile_bits);
 int sv_program_destroy(sv_program* prog);
+/* Compiles, once per program structure, one kernel per pass in which the pass's tile
+ * and register bit positions, op order, control masks and sign tables are literals
+ * (the CUDA runtime compiler, libnvrtc, is loaded at run time); later sv_program_run
+ * calls launch those kernels instead of the interpreting tile kernel.  The result is
+ * the same computation (tests compare both); compilation takes seconds, so this pays
+ * off for programs run many times.  No reference counterpart: qibojit compiles its
+ * fixed kernel set once at import (gpu.py:76-107).  SV_ERR_UNSUPPORTED when libnvrtc
+ * is absent. */
+int sv_program_specialize(sv_context* ctx, sv_program* prog);
 
 /* ---------------------------------------------------------- batched circuits */
 /* Many circuits of uneven size (8..34 qubits) in one job, for variational workloads

@@ -97,6 +97,11 @@ class GB300Backend(_QiboBackend):
         self.tensor_types = (np.ndarray, torch.Tensor)
         self.supports_multigpu = False
         self.fusion = True
+        # execute_circuit specialises a cached complex64 program's pass kernels
+        # (sv_program_specialize) once it has run this many times; None keeps the
+        # interpreting tile kernel.  complex128 passes are FP64-bound: specialising them
+        # does not pay, so they stay interpreted.
+        self.specialize_after: Optional[int] = 2
         self._programs = {}
 
     # ------------------------------------------------------------------ setters
@@ -381,11 +386,22 @@ class GB300Backend(_QiboBackend):
         return Counter(dict(zip(idx.cpu().tolist(), freqs[idx].cpu().tolist())))
 
     # ---------------------------------------------------------------- execution
-    def compile(self, circuit, dtype: Optional[str] = None, tile_bits: int = 0):
-        """Plans ``circuit`` into fused HBM passes (see ``qibojit_gb300.fusion``)."""
+    def compile(self, circuit, dtype: Optional[str] = None, tile_bits: int = 0, specialize: bool = False):
+        """Plans ``circuit`` into fused HBM passes (see ``qibojit_gb300.fusion``); with
+        ``specialize`` also compiles pass kernels for its structure (seconds, once)."""
         from .fusion import FusedProgram
 
-        return FusedProgram(self.ctx, circuit.queue, circuit.nqubits, dtype or self.dtype, tile_bits)
+        dtype = dtype or self.dtype
+        if specialize and not tile_bits:
+            tile_bits = self._specialized_tile_bits(dtype, circuit.nqubits)
+        prog = FusedProgram(self.ctx, circuit.queue, circuit.nqubits, dtype, tile_bits)
+        return prog.specialize() if specialize else prog
+
+    @staticmethod
+    def _specialized_tile_bits(dtype: str, nqubits: int) -> int:
+        """Specialised complex64 passes run fastest on the largest tiles (2^13 amplitudes,
+        512 threads); complex128 keeps the planner's default."""
+        return min(13, nqubits) if dtype == "complex64" else 0
 
     def execute_circuit(self, circuit, initial_state=None, nshots: Optional[int] = None,
                         fuse: Optional[bool] = None):
@@ -411,6 +427,13 @@ class GB300Backend(_QiboBackend):
             prog = self._programs.get(key)
             if prog is None:
                 prog = self.compile(circuit, dtype)
+                self._programs = {key: prog}
+            elif (not prog.specialized and self.specialize_after is not None and prog.runs >= self.specialize_after
+                  and dtype == "complex64"):
+                # a program run repeatedly: re-plan on the larger tile and compile its passes
+                runs = prog.runs
+                prog = self.compile(circuit, dtype, specialize=True)
+                prog.runs = runs
                 self._programs = {key: prog}
             return prog.run(state)
         for gate in circuit.queue:

@@ -47,12 +47,27 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
+def _embed_device_header() -> None:
+    """The run-time pass specialiser compiles generated kernels together with
+    ``csrc/sv_device.cuh``; its text goes into the library as a C string."""
+    with open(os.path.join(CSRC, "sv_device.cuh")) as f:
+        text = f.read()
+    delim = "SVDEVICE"
+    assert f"){delim}\"" not in text
+    out = os.path.join(BUILD, "sv_device_text.inc")
+    body = f'static const char kDeviceHeaderText[] = R"{delim}({text}){delim}";\n'
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
         return LIB
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
-    common = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
+    _embed_device_header()
+    common = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}", f"-I{BUILD}"]
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
@@ -68,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -10,94 +10,9 @@
 #include <stdint.h>
 
 #include "qibojit_gb300.h"
+#include "sv_device.cuh"
 
 namespace sv {
-
-// --------------------------------------------------------------- amplitude types
-template <typename R>
-struct alignas(2 * sizeof(R)) cplx {
-  R re, im;
-};
-
-using c128 = cplx<double>;
-using c64 = cplx<float>;
-
-template <typename T> struct real_of { using type = T; };
-template <typename R> struct real_of<cplx<R>> { using type = R; };
-
-template <typename T> struct is_complex { static constexpr bool value = false; };
-template <typename R> struct is_complex<cplx<R>> { static constexpr bool value = true; };
-
-template <typename R>
-__host__ __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
-  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
-template <typename R>
-__host__ __device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) {
-  return {a.re + b.re, a.im + b.im};
-}
-// a*x + b*y, the shape of every dense gate row
-template <typename R>
-__device__ __forceinline__ cplx<R> cmad2(cplx<R> a, cplx<R> x, cplx<R> b, cplx<R> y) {
-  cplx<R> r;
-  r.re = fma(a.re, x.re, fma(-a.im, x.im, fma(b.re, y.re, -b.im * y.im)));
-  r.im = fma(a.re, x.im, fma(a.im, x.re, fma(b.re, y.im, b.im * y.re)));
-  return r;
-}
-template <typename R>
-__device__ __forceinline__ cplx<R> cfma(cplx<R> a, cplx<R> x, cplx<R> acc) {
-  acc.re = fma(a.re, x.re, fma(-a.im, x.im, acc.re));
-  acc.im = fma(a.re, x.im, fma(a.im, x.re, acc.im));
-  return acc;
-}
-template <typename R> __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
-
-// generic helpers usable for both real and complex amplitude types
-template <typename T> __device__ __forceinline__ T tmul(T a, T b) { return a * b; }
-template <> __device__ __forceinline__ c128 tmul<c128>(c128 a, c128 b) { return cmul(a, b); }
-template <> __device__ __forceinline__ c64 tmul<c64>(c64 a, c64 b) { return cmul(a, b); }
-template <typename T> __device__ __forceinline__ T tfma(T a, T x, T acc) { return fma(a, x, acc); }
-template <> __device__ __forceinline__ c128 tfma<c128>(c128 a, c128 x, c128 acc) { return cfma(a, x, acc); }
-template <> __device__ __forceinline__ c64 tfma<c64>(c64 a, c64 x, c64 acc) { return cfma(a, x, acc); }
-template <typename T> __device__ __forceinline__ T tzero() { return T(0); }
-template <> __device__ __forceinline__ c128 tzero<c128>() { return {0.0, 0.0}; }
-template <> __device__ __forceinline__ c64 tzero<c64>() { return {0.0f, 0.0f}; }
-template <typename T> __device__ __forceinline__ T tneg(T a) { return -a; }
-template <> __device__ __forceinline__ c128 tneg<c128>(c128 a) { return {-a.re, -a.im}; }
-template <> __device__ __forceinline__ c64 tneg<c64>(c64 a) { return {-a.re, -a.im}; }
-template <typename T> __device__ __forceinline__ double tnorm2(T a) { return (double)a * (double)a; }
-template <> __device__ __forceinline__ double tnorm2<c128>(c128 a) { return a.re * a.re + a.im * a.im; }
-template <> __device__ __forceinline__ double tnorm2<c64>(c64 a) {
-  return (double)a.re * (double)a.re + (double)a.im * (double)a.im;
-}
-
-// streaming loads/stores: each amplitude is touched once per pass
-template <typename T> __device__ __forceinline__ T ldg_stream(const T* p) { return __ldcs(p); }
-template <> __device__ __forceinline__ c128 ldg_stream<c128>(const c128* p) {
-  double2 v = __ldcs(reinterpret_cast<const double2*>(p));
-  return {v.x, v.y};
-}
-template <> __device__ __forceinline__ c64 ldg_stream<c64>(const c64* p) {
-  float2 v = __ldcs(reinterpret_cast<const float2*>(p));
-  return {v.x, v.y};
-}
-// read-only cached load (operands reused by many threads)
-template <typename T> __device__ __forceinline__ T ldg_ro(const T* p) { return __ldg(p); }
-template <> __device__ __forceinline__ c128 ldg_ro<c128>(const c128* p) {
-  double2 v = __ldg(reinterpret_cast<const double2*>(p));
-  return {v.x, v.y};
-}
-template <> __device__ __forceinline__ c64 ldg_ro<c64>(const c64* p) {
-  float2 v = __ldg(reinterpret_cast<const float2*>(p));
-  return {v.x, v.y};
-}
-template <typename T> __device__ __forceinline__ void stg_stream(T* p, T v) { __stcs(p, v); }
-template <> __device__ __forceinline__ void stg_stream<c128>(c128* p, c128 v) {
-  __stcs(reinterpret_cast<double2*>(p), make_double2(v.re, v.im));
-}
-template <> __device__ __forceinline__ void stg_stream<c64>(c64* p, c64 v) {
-  __stcs(reinterpret_cast<float2*>(p), make_float2(v.re, v.im));
-}
 
 // ----------------------------------------------------------------- index maps
 constexpr int kMaxQubits = 40;     // largest state the engine addresses (2^40 amplitudes)

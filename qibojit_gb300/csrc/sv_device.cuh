@@ -1,0 +1,204 @@
+// sv_device.cuh -- device code shared by the compiled kernels and by the pass
+// kernels specialised at run time.
+//
+// Amplitude types and their arithmetic, the shared-memory tile index map, cp.async
+// wrappers and the register-level gate ops (a thread's 16 amplitudes of one phase).
+// The file is self-contained (no includes, no host-only types) so the engine can hand
+// its text to the CUDA runtime compiler unchanged.
+#pragma once
+
+namespace sv {
+
+// --------------------------------------------------------------- amplitude types
+template <typename R>
+struct alignas(2 * sizeof(R)) cplx {
+  R re, im;
+};
+
+using c128 = cplx<double>;
+using c64 = cplx<float>;
+
+template <typename T> struct real_of { using type = T; };
+template <typename R> struct real_of<cplx<R>> { using type = R; };
+
+template <typename T> struct is_complex { static constexpr bool value = false; };
+template <typename R> struct is_complex<cplx<R>> { static constexpr bool value = true; };
+
+template <typename R>
+__host__ __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename R>
+__host__ __device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) {
+  return {a.re + b.re, a.im + b.im};
+}
+// a*x + b*y, the shape of every dense gate row
+template <typename R>
+__device__ __forceinline__ cplx<R> cmad2(cplx<R> a, cplx<R> x, cplx<R> b, cplx<R> y) {
+  cplx<R> r;
+  r.re = fma(a.re, x.re, fma(-a.im, x.im, fma(b.re, y.re, -b.im * y.im)));
+  r.im = fma(a.re, x.im, fma(a.im, x.re, fma(b.re, y.im, b.im * y.re)));
+  return r;
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cfma(cplx<R> a, cplx<R> x, cplx<R> acc) {
+  acc.re = fma(a.re, x.re, fma(-a.im, x.im, acc.re));
+  acc.im = fma(a.re, x.im, fma(a.im, x.re, acc.im));
+  return acc;
+}
+template <typename R> __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
+
+// generic helpers usable for both real and complex amplitude types
+template <typename T> __device__ __forceinline__ T tmul(T a, T b) { return a * b; }
+template <> __device__ __forceinline__ c128 tmul<c128>(c128 a, c128 b) { return cmul(a, b); }
+template <> __device__ __forceinline__ c64 tmul<c64>(c64 a, c64 b) { return cmul(a, b); }
+template <typename T> __device__ __forceinline__ T tfma(T a, T x, T acc) { return fma(a, x, acc); }
+template <> __device__ __forceinline__ c128 tfma<c128>(c128 a, c128 x, c128 acc) { return cfma(a, x, acc); }
+template <> __device__ __forceinline__ c64 tfma<c64>(c64 a, c64 x, c64 acc) { return cfma(a, x, acc); }
+template <typename T> __device__ __forceinline__ T tzero() { return T(0); }
+template <> __device__ __forceinline__ c128 tzero<c128>() { return {0.0, 0.0}; }
+template <> __device__ __forceinline__ c64 tzero<c64>() { return {0.0f, 0.0f}; }
+template <typename T> __device__ __forceinline__ T tneg(T a) { return -a; }
+template <> __device__ __forceinline__ c128 tneg<c128>(c128 a) { return {-a.re, -a.im}; }
+template <> __device__ __forceinline__ c64 tneg<c64>(c64 a) { return {-a.re, -a.im}; }
+template <typename T> __device__ __forceinline__ double tnorm2(T a) { return (double)a * (double)a; }
+template <> __device__ __forceinline__ double tnorm2<c128>(c128 a) { return a.re * a.re + a.im * a.im; }
+template <> __device__ __forceinline__ double tnorm2<c64>(c64 a) {
+  return (double)a.re * (double)a.re + (double)a.im * (double)a.im;
+}
+
+// streaming loads/stores: each amplitude is touched once per pass
+template <typename T> __device__ __forceinline__ T ldg_stream(const T* p) { return __ldcs(p); }
+template <> __device__ __forceinline__ c128 ldg_stream<c128>(const c128* p) {
+  double2 v = __ldcs(reinterpret_cast<const double2*>(p));
+  return {v.x, v.y};
+}
+template <> __device__ __forceinline__ c64 ldg_stream<c64>(const c64* p) {
+  float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+// read-only cached load (operands reused by many threads)
+template <typename T> __device__ __forceinline__ T ldg_ro(const T* p) { return __ldg(p); }
+template <> __device__ __forceinline__ c128 ldg_ro<c128>(const c128* p) {
+  double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  return {v.x, v.y};
+}
+template <> __device__ __forceinline__ c64 ldg_ro<c64>(const c64* p) {
+  float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+template <typename T> __device__ __forceinline__ void stg_stream(T* p, T v) { __stcs(p, v); }
+template <> __device__ __forceinline__ void stg_stream<c128>(c128* p, c128 v) {
+  __stcs(reinterpret_cast<double2*>(p), make_double2(v.re, v.im));
+}
+template <> __device__ __forceinline__ void stg_stream<c64>(c64* p, c64 v) {
+  __stcs(reinterpret_cast<float2*>(p), make_float2(v.re, v.im));
+}
+
+// ------------------------------------------------------------ shared-memory tile
+// element e of a tile sits at e + e/16: one padding slot per 16, so the 16-amplitude
+// columns of a phase fall into different banks
+__device__ __forceinline__ int smem_pos(int e) { return e + (e >> 4); }
+
+// ------------------------------------------------------------------ cp.async
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem_src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// ---------------------------------------------------------------- register ops
+template <typename T, int U>
+__device__ __forceinline__ void dense1_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+  const T a = m[0], b = m[1], c = m[2], d = m[3];
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const int k = j | (1 << U);
+    const T x = v[j], y = v[k];
+    v[j] = tfma(a, x, tmul(b, y));
+    v[k] = tfma(c, x, tmul(d, y));
+  }
+}
+
+template <typename T, int U0, int U1>
+__device__ __forceinline__ void dense2_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & ((1 << U0) | (1 << U1))) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const int i1 = j | (1 << U1), i2 = j | (1 << U0), i3 = j | (1 << U0) | (1 << U1);
+    const T x0 = v[j], x1 = v[i1], x2 = v[i2], x3 = v[i3];
+    T o[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      T acc = tmul(m[4 * r + 3], x3);
+      acc = tfma(m[4 * r + 2], x2, acc);
+      acc = tfma(m[4 * r + 1], x1, acc);
+      o[r] = tfma(m[4 * r + 0], x0, acc);
+    }
+    v[j] = o[0];
+    v[i1] = o[1];
+    v[i2] = o[2];
+    v[i3] = o[3];
+  }
+}
+
+template <typename T, int U>
+__device__ __forceinline__ void x1_regs(T (&v)[16], unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const T t = v[j];
+    v[j] = v[j | (1 << U)];
+    v[j | (1 << U)] = t;
+  }
+}
+
+// real 2x2 on complex amplitudes: coefficients' imaginary parts are zero
+template <typename T, int U>
+__device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+  if constexpr (is_complex<T>::value) {
+    const auto a = m[0].re, b = m[1].re, c = m[2].re, d = m[3].re;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      if (j & (1 << U)) continue;
+      if (!((jm >> j) & 1u)) continue;
+      const int k = j | (1 << U);
+      const T x = v[j], y = v[k];
+      v[j].re = fma(a, x.re, b * y.re);
+      v[j].im = fma(a, x.im, b * y.im);
+      v[k].re = fma(c, x.re, d * y.re);
+      v[k].im = fma(c, x.im, d * y.im);
+    }
+  }
+}
+
+template <typename T, int U0, int U1>
+__device__ __forceinline__ void swap2_regs(T (&v)[16], unsigned jm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & ((1 << U0) | (1 << U1))) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const T t = v[j | (1 << U1)];
+    v[j | (1 << U1)] = v[j | (1 << U0)];
+    v[j | (1 << U0)] = t;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void apply_negations(T (&v)[16], unsigned nm) {
+#pragma unroll
+  for (int j = 0; j < 16; j++)
+    if ((nm >> j) & 1u) v[j] = tneg(v[j]);
+}
+
+}  // namespace sv

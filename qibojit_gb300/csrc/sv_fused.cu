@@ -25,123 +25,11 @@
 #include <algorithm>
 #include <vector>
 
-#include "sv_common.cuh"
+#include "sv_plan.cuh"
 
 namespace sv {
 
-constexpr int kRB = 4;            // register bits per phase (16 amplitudes per thread)
-constexpr int kMaxTile = 14;      // tile bits
-constexpr int kLowBits = 4;       // lowest bits always in a tile (contiguous runs)
-constexpr int kMaxPassOps = 128;  // ops (and phases) per pass
-constexpr int kCoefBytes = 12288; // coefficient bytes per pass
-
-enum : uint8_t {
-  FOP_DENSE1 = 0,   // complex 2x2
-  FOP_DENSE2 = 1,   // complex 4x4
-  FOP_DIAG = 2,     // diagonal phases on up to 3 bits
-  FOP_SIGN = 3,     // diagonal with entries +-1 (CZ, Z, CCZ): folded into a negate mask
-  FOP_D1RUN = 4,    // up to 4 uncontrolled complex 2x2 on distinct register bits
-  FOP_X1 = 5,       // X (CNOT, Toffoli targets): a register swap, no arithmetic
-  FOP_DENSE1R = 6,  // real 2x2 (RY, H): half the flops of a complex one
-  FOP_SWAP2 = 7,    // SWAP: exchange of |01> and |10>, no arithmetic
-  FOP_GRADX = 8,    // adjoint sweep: Im<lambda|X_q|psi> on a register bit (coef = parameter index)
-  FOP_GRADY = 9,    //                Im<lambda|Y_q|psi>
-  FOP_GRADZ = 10    //                Im<lambda|Z_q|psi>, any bit (diagonal)
-};
-// internal op kind of the adjoint planner: a gradient marker (no matrix)
-constexpr int OP_GRAD = 2;
-enum : uint8_t { FLAG_OMASK = 1, FLAG_TMASK = 2 };
-
-// One op in phase-local form (64 bytes).
-struct FOp {
-  uint8_t type, u0, u1, nd;  // dense: register positions of the targets (u0 = row MSB); diag: #bits
-  int8_t tb[3];              // diag bit i read from the thread's local index bit tb[i] (or -1)
-  int8_t ob[3];              // diag bit i read from the tile's outer global bit ob[i] (or -1)
-  uint8_t pad0[2];
-  uint16_t jmask;            // register-level controls: amplitudes / pair bases j allowed
-  uint16_t pad1;
-  uint32_t tmask;            // thread-level controls: local non-register bits that must be 1
-  uint32_t coef;             // first coefficient of this op in the pass's coefficient array
-  uint64_t omask;            // tile-level controls: outer global bits that must be 1
-  uint64_t rpart;            // diag: table-index part from register bits, 4 bits per amplitude j
-  uint16_t neg[8];           // sign diag: negate-mask over j for each non-register index part
-  uint8_t flags;             // FLAG_OMASK / FLAG_TMASK: which control checks apply
-  uint8_t nrun;              // FOP_D1RUN: number of uncontrolled one-target gates (1..4)
-  uint8_t ru[4];             // FOP_D1RUN: their register positions; matrices at coef + 4k
-  uint8_t pad2[2];
-};
-static_assert(sizeof(FOp) == 64, "FOp layout");
-
-struct Phase {
-  uint8_t rb[kRB];           // local tile bits held in registers, ascending (j bit u <-> rb[u])
-  uint16_t op_begin, op_end;
-  uint16_t soff[16];         // shared-memory offset of register j: smem_pos(register bits of j)
-};
-
-template <typename T>
-struct PassParams {
-  int32_t n, kt, nphases, nops;
-  int64_t ntiles;
-  int32_t tile_pos[kMaxTile];  // global bit positions of the tile bits, ascending
-  int32_t coef_goff;           // batched runs: this pass's first coefficient in a circuit's block
-  Phase phases[kMaxPassOps];
-  FOp ops[kMaxPassOps];
-  T coef[kCoefBytes / sizeof(T)];
-};
-
-__device__ __forceinline__ int smem_pos(int e) { return e + (e >> 4); }
-
-// ------------------------------------------------------------------ cp.async
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-  if constexpr (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem_src), "n"(BYTES) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// ---------------------------------------------------------------- register ops
-template <typename T, int U>
-__device__ __forceinline__ void dense1_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
-  const T a = m[0], b = m[1], c = m[2], d = m[3];
-#pragma unroll
-  for (int j = 0; j < 16; j++) {
-    if (j & (1 << U)) continue;
-    if (!((jm >> j) & 1u)) continue;
-    const int k = j | (1 << U);
-    const T x = v[j], y = v[k];
-    v[j] = tfma(a, x, tmul(b, y));
-    v[k] = tfma(c, x, tmul(d, y));
-  }
-}
-
-template <typename T, int U0, int U1>
-__device__ __forceinline__ void dense2_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
-#pragma unroll
-  for (int j = 0; j < 16; j++) {
-    if (j & ((1 << U0) | (1 << U1))) continue;
-    if (!((jm >> j) & 1u)) continue;
-    const int i1 = j | (1 << U1), i2 = j | (1 << U0), i3 = j | (1 << U0) | (1 << U1);
-    const T x0 = v[j], x1 = v[i1], x2 = v[i2], x3 = v[i3];
-    T o[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      T acc = tmul(m[4 * r + 3], x3);
-      acc = tfma(m[4 * r + 2], x2, acc);
-      acc = tfma(m[4 * r + 1], x1, acc);
-      o[r] = tfma(m[4 * r + 0], x0, acc);
-    }
-    v[j] = o[0];
-    v[i1] = o[1];
-    v[i2] = o[2];
-    v[i3] = o[3];
-  }
-}
-
+// ------------------------------------------------- register ops at run-time positions
 template <typename T>
 __device__ __forceinline__ void dense1_dispatch(T (&v)[16], const T* m, int u, unsigned jm) {
   // jm == 0xffff marks an op without register-level controls: no per-pair tests
@@ -159,49 +47,6 @@ __device__ __forceinline__ void dense1_dispatch(T (&v)[16], const T* m, int u, u
     case 1: dense1_regs<T, 1>(v, m, jm); break;
     case 2: dense1_regs<T, 2>(v, m, jm); break;
     default: dense1_regs<T, 3>(v, m, jm); break;
-  }
-}
-
-template <typename T, int U>
-__device__ __forceinline__ void x1_regs(T (&v)[16], unsigned jm) {
-#pragma unroll
-  for (int j = 0; j < 16; j++) {
-    if (j & (1 << U)) continue;
-    if (!((jm >> j) & 1u)) continue;
-    const T t = v[j];
-    v[j] = v[j | (1 << U)];
-    v[j | (1 << U)] = t;
-  }
-}
-
-// real 2x2 on complex amplitudes: coefficients' imaginary parts are zero
-template <typename T, int U>
-__device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
-  if constexpr (is_complex<T>::value) {
-    const auto a = m[0].re, b = m[1].re, c = m[2].re, d = m[3].re;
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-      if (j & (1 << U)) continue;
-      if (!((jm >> j) & 1u)) continue;
-      const int k = j | (1 << U);
-      const T x = v[j], y = v[k];
-      v[j].re = fma(a, x.re, b * y.re);
-      v[j].im = fma(a, x.im, b * y.im);
-      v[k].re = fma(c, x.re, d * y.re);
-      v[k].im = fma(c, x.im, d * y.im);
-    }
-  }
-}
-
-template <typename T, int U0, int U1>
-__device__ __forceinline__ void swap2_regs(T (&v)[16], unsigned jm) {
-#pragma unroll
-  for (int j = 0; j < 16; j++) {
-    if (j & ((1 << U0) | (1 << U1))) continue;
-    if (!((jm >> j) & 1u)) continue;
-    const T t = v[j | (1 << U1)];
-    v[j | (1 << U1)] = v[j | (1 << U0)];
-    v[j | (1 << U0)] = t;
   }
 }
 
@@ -232,13 +77,6 @@ __device__ __forceinline__ void swap2_dispatch(T (&v)[16], int u0, int u1, unsig
   if (a == A && b == B) { swap2_regs<T, A, B>(v, jm); return; }
   SV_S2(0, 1) SV_S2(0, 2) SV_S2(0, 3) SV_S2(1, 2) SV_S2(1, 3) SV_S2(2, 3)
 #undef SV_S2
-}
-
-template <typename T>
-__device__ __forceinline__ void apply_negations(T (&v)[16], unsigned nm) {
-#pragma unroll
-  for (int j = 0; j < 16; j++)
-    if ((nm >> j) & 1u) v[j] = tneg(v[j]);
 }
 
 template <typename T>
@@ -421,48 +259,6 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
 }
 
 // =================================================================== planner
-struct HostOp {
-  int kind;                 // SV_OP_DENSE / SV_OP_DIAG
-  int nt;                   // targets
-  int tpos[kMaxTargets];    // global bit positions of the targets, gate order
-  int nc;
-  int cpos[16];
-  std::vector<double> m;    // complex entries (re, im) pairs
-  bool sign_only = false;   // diagonal with entries in {+1, -1}
-  int sign_mask = 0;        // bit i set: entry i is -1
-  bool is_x = false;        // dense one-target [[0, 1], [1, 0]]
-  bool is_real = false;     // dense with all-real entries
-  bool is_swap = false;     // dense two-target SWAP
-  int gen = 0;              // OP_GRAD: generator 1 = X, 2 = Y, 3 = Z
-  int param = -1;           // OP_GRAD: parameter index
-};
-
-// ops that need their target bit in the tile and in the phase's registers
-static inline bool dense_like(const HostOp& h) { return h.kind == SV_OP_DENSE || (h.kind == OP_GRAD && h.gen != 3); }
-
-struct Segment {
-  bool fused = false;
-  int pass = -1;            // index into the program's pass parameter blocks
-  int host_op = -1;         // unfused op
-};
-
-}  // namespace sv
-
-struct sv_program {
-  int dtype, nqubits, kt;
-  std::vector<sv::HostOp> ops;
-  std::vector<sv::Segment> segments;
-  std::vector<unsigned char> passes;  // PassParams<T> blocks, back to back
-  size_t pass_bytes = 0;
-  // coefficient sources of all passes, back to back: (op index, entry) per slot
-  std::vector<int32_t> coef_src;
-  std::vector<size_t> pass_coef_off;
-  size_t coef_total = 0;
-  int npasses = 0, nunfused = 0, nfused_gates = 0, nphases = 0;
-};
-
-namespace sv {
-
 template <typename T>
 static T to_elem(const double* re_im) {
   if constexpr (is_complex<T>::value) {
@@ -880,11 +676,6 @@ static int build_program(sv_program* prog) {
   return SV_OK;
 }
 
-template <typename T>
-static size_t pass_smem(int kt) {
-  const int tsize = 1 << kt;
-  return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
-}
 
 template <typename T, int MAXT, int MINB, bool BATCHED>
 static int launch_variant(Context* ctx, cudaStream_t stream, const PassParams<T>& p, void* state, int threads,
@@ -935,7 +726,8 @@ static int run_program(Context* ctx, const sv_program* prog, void* state) {
     if (s.fused) {
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
-      SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles, ctx->stream));
+      if (prog->spec) SV_TRY(specialized_launch(ctx, prog, s.pass, state));
+      else SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles, ctx->stream));
     } else {
       const HostOp& h = prog->ops[s.host_op];
       std::vector<int32_t> targets(h.nt), qubits;
@@ -1141,6 +933,7 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
 }
 
 int sv_program_destroy(sv_program* prog) {
+  if (prog && prog->spec) specialized_free(prog->spec);
   delete prog;
   return SV_OK;
 }

@@ -1,0 +1,441 @@
+// sv_specialize.cu -- pass kernels compiled at run time for one program's structure.
+//
+// The tile kernel of sv_fused.cu interprets a pass: every phase and op is decoded
+// from the kernel parameters, register positions go through switch tables, shared-
+// memory offsets are loaded per amplitude.  For a program that runs many times (the
+// same circuit with new parameters, or repeated shots of one circuit) the engine can
+// instead emit CUDA C++ for each pass with all of that fixed: tile and register bit
+// positions, offsets, op order and kinds, control masks and sign tables become
+// literals, and the gate coefficients are read straight from the kernel parameters.
+// The source is compiled for sm_103a by the CUDA runtime compiler (NVRTC, loaded
+// with dlopen so the library has no link-time dependency on it), loaded with
+// cudaLibraryLoadData and launched like the interpreted pass: same tiles, same
+// double-buffered cp.async staging, same register ops (sv_device.cuh, whose text is
+// compiled into this library).  Compiled kernels are cached per process by their
+// source text, which holds no coefficient values.
+#include <dlfcn.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <condition_variable>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "sv_plan.cuh"
+#include "sv_device_text.inc"  // kDeviceHeaderText: sv_device.cuh as a string (generated at build time)
+
+namespace sv {
+
+// ------------------------------------------------------------- NVRTC (dlopen)
+namespace {
+
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram* nvrtcProgram_t;
+
+struct Nvrtc {
+  void* handle = nullptr;
+  nvrtcResult_t (*create)(nvrtcProgram_t*, const char*, const char*, int, const char* const*,
+                          const char* const*) = nullptr;
+  nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char* const*) = nullptr;
+  nvrtcResult_t (*destroy)(nvrtcProgram_t*) = nullptr;
+  nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t*) = nullptr;
+  nvrtcResult_t (*log)(nvrtcProgram_t, char*) = nullptr;
+  nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t*) = nullptr;
+  nvrtcResult_t (*cubin)(nvrtcProgram_t, char*) = nullptr;
+  bool ok = false;
+};
+
+const Nvrtc& nvrtc() {
+  static Nvrtc api;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                           "/usr/local/cuda/lib64/libnvrtc.so"};
+    for (const char* nm : names) {
+      api.handle = dlopen(nm, RTLD_NOW | RTLD_LOCAL);
+      if (api.handle) break;
+    }
+    if (!api.handle) return;
+    auto sym = [](const char* s) { return dlsym(api.handle, s); };
+    api.create = (decltype(api.create))sym("nvrtcCreateProgram");
+    api.compile = (decltype(api.compile))sym("nvrtcCompileProgram");
+    api.destroy = (decltype(api.destroy))sym("nvrtcDestroyProgram");
+    api.log_size = (decltype(api.log_size))sym("nvrtcGetProgramLogSize");
+    api.log = (decltype(api.log))sym("nvrtcGetProgramLog");
+    api.cubin_size = (decltype(api.cubin_size))sym("nvrtcGetCUBINSize");
+    api.cubin = (decltype(api.cubin))sym("nvrtcGetCUBIN");
+    api.ok = api.create && api.compile && api.destroy && api.log_size && api.log && api.cubin_size && api.cubin;
+  });
+  return api;
+}
+
+// ---------------------------------------------------------------- generator
+// `var`'s bit i moved to bit pos[i], as one shift-and-mask term per run of consecutive positions
+std::string deposit_expr(const char* var, const std::vector<int>& pos, bool wide) {
+  std::ostringstream o;
+  size_t i = 0;
+  bool first = true;
+  while (i < pos.size()) {
+    size_t j = i + 1;
+    while (j < pos.size() && pos[j] == pos[j - 1] + 1) j++;
+    const long long mask = (1ll << (j - i)) - 1;
+    o << (first ? "" : " | ") << "((" << (wide ? "(long long)" : "") << "(" << var << " >> " << i << ") & " << mask
+      << (wide ? "ll" : "") << ") << " << pos[i] << ")";
+    first = false;
+    i = j;
+  }
+  if (first) o << "0";
+  return o.str();
+}
+
+int coef_count(const FOp& f) {
+  switch (f.type) {
+    case FOP_D1RUN: return (int)f.coef + 4 * f.nrun;
+    case FOP_DENSE1:
+    case FOP_DENSE1R: return (int)f.coef + 4;
+    case FOP_DENSE2: return (int)f.coef + 16;
+    case FOP_DIAG: return (int)f.coef + (1 << f.nd);
+    default: return 0;
+  }
+}
+
+struct KernelShape {
+  int threads, maxt, minb;
+  size_t smem;
+};
+
+template <typename T>
+KernelShape shape_of(int kt) {
+  KernelShape k;
+  k.threads = 1 << (kt - kRB);
+  k.maxt = k.threads <= 256 ? 256 : 512;
+  k.minb = (sizeof(T) < 16 && k.threads <= 256) ? 3 : 1;  // the interpreted pass's launch variants
+  k.smem = 2 * sizeof(T) * (size_t)((1 << kt) + (1 << (kt - kLowBits)));
+  return k;
+}
+
+// CUDA source of one pass: kernel `name`, coefficients in a by-value parameter struct
+template <typename T>
+std::string pass_source(const PassParams<T>& p, const char* name) {
+  std::ostringstream o;
+  const char* ty = sizeof(T) == 16 ? "sv::c128" : "sv::c64";
+  const int kt = p.kt, n = p.n;
+  const KernelShape ks = shape_of<T>(kt);
+  const int nth = ks.threads;
+  int ncoef = 1;
+  for (int q = 0; q < p.nops; q++) ncoef = std::max(ncoef, coef_count(p.ops[q]));
+  std::vector<int> tpos(p.tile_pos, p.tile_pos + kt), outer;
+  for (int g = 0; g < n; g++)
+    if (std::find(tpos.begin(), tpos.end(), g) == tpos.end()) outer.push_back(g);
+  const std::vector<int> low(tpos.begin(), tpos.begin() + (kt - kRB));
+  o << "struct " << name << "_coef { " << ty << " c[" << ncoef << "]; };\n"
+    << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
+    << "* __restrict__ state, const __grid_constant__ " << name << "_coef cf) {\n"
+    << "  using T = " << ty << ";\n"
+    << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n"
+    << "  T* const buf0 = reinterpret_cast<T*>(smem_raw);\n"
+    << "  constexpr int TSTRIDE = " << ((1 << kt) + (1 << (kt - kLowBits))) << ", SK = " << (nth + nth / 16) << ";\n"
+    << "  const int tid = threadIdx.x;\n"
+    // tile element e = tid + k * threads: its low bits are tid's, its top four bits k's
+    << "  const long long dtid = " << deposit_expr("tid", low, true) << ";\n"
+    << "  const int stid = tid + (tid >> 4);\n"
+    << "  constexpr long long DEPK[16] = {";
+  for (int k = 0; k < 16; k++) {
+    long long d = 0;
+    for (int i = 0; i < 4; i++)
+      if ((k >> i) & 1) d |= 1ll << tpos[kt - kRB + i];
+    o << d << "ll" << (k < 15 ? ", " : "};\n");
+  }
+  o << "  const long long nitems = " << p.ntiles << "ll;\n"
+    << "  auto origin = [&](long long t) -> long long { return " << deposit_expr("t", outer, true) << "; };\n"
+    << "  auto issue_load = [&](T* buf, long long base) {\n"
+    << "#pragma unroll\n"
+    << "    for (int k = 0; k < 16; k++)\n"
+    << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, state + (base | dtid | DEPK[k]));\n"
+    << "    sv::cp_async_commit();\n"
+    << "  };\n"
+    << "  long long t = blockIdx.x;\n"
+    << "  if (t < nitems) issue_load(buf0, origin(t));\n"
+    << "  int cur = 0;\n"
+    << "  for (; t < nitems; t += gridDim.x, cur ^= 1) {\n"
+    << "    T* const tile = buf0 + cur * TSTRIDE;\n"
+    << "    const long long base = origin(t);\n"
+    << "    const long long tn = t + gridDim.x;\n"
+    << "    if (tn < nitems) {\n"
+    << "      issue_load(buf0 + (cur ^ 1) * TSTRIDE, origin(tn));\n"
+    << "      sv::cp_async_wait<1>();\n"
+    << "    } else {\n"
+    << "      sv::cp_async_wait<0>();\n"
+    << "    }\n"
+    << "    __syncthreads();\n";
+  for (int ph = 0; ph < p.nphases; ph++) {
+    const Phase& P = p.phases[ph];
+    std::vector<int> nonreg;
+    for (int b = 0; b < kt; b++)
+      if (b != P.rb[0] && b != P.rb[1] && b != P.rb[2] && b != P.rb[3]) nonreg.push_back(b);
+    o << "    {  // phase " << ph << ", register bits " << (int)P.rb[0] << " " << (int)P.rb[1] << " "
+      << (int)P.rb[2] << " " << (int)P.rb[3] << "\n"
+      << "      const int lbase = " << deposit_expr("tid", nonreg, false) << ";\n"
+      << "      (void)lbase;\n"
+      << "      T* const tp = tile + lbase + (lbase >> 4);\n"
+      << "      T v[16];\n";
+    for (int j = 0; j < 16; j++) o << "      v[" << j << "] = tp[" << P.soff[j] << "];\n";
+    bool uses_pn = false;
+    for (int q = P.op_begin; q < P.op_end; q++) uses_pn |= p.ops[q].type == FOP_SIGN;
+    if (uses_pn) o << "      unsigned pn = 0;\n";
+    unsigned stat = 0;  // negations known at compile time
+    bool dyn = false;   // run-time negations pending in pn
+    auto flush = [&]() {
+      for (int j = 0; j < 16; j++)
+        if ((stat >> j) & 1) o << "      v[" << j << "] = sv::tneg(v[" << j << "]);\n";
+      stat = 0;
+      if (dyn) o << "      sv::apply_negations(v, pn);\n      pn = 0;\n";
+      dyn = false;
+    };
+    for (int q = P.op_begin; q < P.op_end; q++) {
+      const FOp& f = p.ops[q];
+      std::ostringstream c;
+      if (f.type != FOP_D1RUN) {
+        if (f.omask) c << "((base & " << (long long)f.omask << "ll) == " << (long long)f.omask << "ll)";
+        if (f.tmask) c << (f.omask ? " && " : "") << "((lbase & " << f.tmask << ") == " << f.tmask << ")";
+      }
+      const std::string cond = c.str();
+      const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
+      if (f.type == FOP_D1RUN || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R || f.type == FOP_X1 ||
+          f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
+        flush();
+      // non-register part of a diagonal's table index
+      std::ostringstream te;
+      bool tany = false;
+      for (int i = 0; i < f.nd; i++) {
+        const int sh = f.nd - 1 - i;
+        if (f.tb[i] >= 0) te << (tany ? " | " : "") << "(((lbase >> " << (int)f.tb[i] << ") & 1) << " << sh << ")";
+        else if (f.ob[i] >= 0) te << (tany ? " | " : "") << "((int)((base >> " << (int)f.ob[i] << ") & 1) << " << sh << ")";
+        else continue;
+        tany = true;
+      }
+      switch (f.type) {
+        case FOP_D1RUN:
+          for (int k = 0; k < f.nrun; k++)
+            o << "      sv::dense1_regs<T, " << (int)f.ru[k] << ">(v, cf.c + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+          break;
+        case FOP_DENSE1:
+          o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
+          break;
+        case FOP_DENSE1R:
+          o << pre << "sv::dense1r_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
+          break;
+        case FOP_X1:
+          o << pre << "sv::x1_regs<T, " << (int)f.u0 << ">(v, " << f.jmask << "u);\n";
+          break;
+        case FOP_SWAP2:
+          o << pre << "sv::swap2_regs<T, " << (int)std::min(f.u0, f.u1) << ", " << (int)std::max(f.u0, f.u1) << ">(v, "
+            << f.jmask << "u);\n";
+          break;
+        case FOP_DENSE2:
+          o << pre << "sv::dense2_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, cf.c + " << f.coef << ", "
+            << f.jmask << "u);\n";
+          break;
+        case FOP_SIGN:
+          if (!tany && cond.empty()) {
+            stat ^= f.neg[0];
+          } else {
+            unsigned long long lo = 0, hi = 0;
+            for (int t2 = 0; t2 < 8; t2++) (t2 < 4 ? lo : hi) |= (unsigned long long)f.neg[t2] << (16 * (t2 & 3));
+            o << pre << "{\n        const int ti = " << (tany ? te.str() : std::string("0")) << ";\n"
+              << "        pn ^= (unsigned)(((ti < 4) ? (" << lo << "ull >> (16 * ti)) : (" << hi
+              << "ull >> (16 * (ti - 4)))) & 0xffffull);\n      }\n";
+            dyn = true;
+          }
+          break;
+        case FOP_DIAG:
+          o << pre << "{\n        const int ti = " << (tany ? te.str() : std::string("0")) << ";\n        (void)ti;\n";
+          for (int j = 0; j < 16; j++) {
+            if (!((f.jmask >> j) & 1)) continue;
+            const int r = (int)((f.rpart >> (4 * j)) & 15);
+            o << "        v[" << j << "] = sv::tmul(cf.c[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
+          }
+          o << "      }\n";
+          break;
+        default:
+          return std::string();  // gradient markers and anything else: not specialisable
+      }
+    }
+    flush();
+    for (int j = 0; j < 16; j++) o << "      tp[" << P.soff[j] << "] = v[" << j << "];\n";
+    o << "      __syncthreads();\n    }\n";
+  }
+  o << "#pragma unroll\n"
+    << "    for (int k = 0; k < 16; k++) sv::stg_stream(state + (base | dtid | DEPK[k]), tile[stid + k * SK]);\n"
+    << "    __syncthreads();  // this buffer is refilled by the prefetch two tiles later\n"
+    << "  }\n}\n";
+  return o.str();
+}
+
+// ---------------------------------------------------------------- kernel cache
+struct CompiledKernel {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+};
+
+std::mutex g_cache_mutex;
+std::unordered_map<std::string, CompiledKernel>& cache() {
+  static std::unordered_map<std::string, CompiledKernel> c;
+  return c;
+}
+
+// NVRTC: source -> cubin for sm_103a
+int compile_cubin(const std::string& body, std::vector<char>* cubin, std::string* log) {
+  const Nvrtc& api = nvrtc();
+  const std::string src = std::string(kDeviceHeaderText) + "\n" + body;
+  nvrtcProgram_t prog = nullptr;
+  if (api.create(&prog, src.c_str(), "sv_pass.cu", 0, nullptr, nullptr) != 0) {
+    *log = "nvrtcCreateProgram failed";
+    return SV_ERR_CUDA;
+  }
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--diag-suppress=177"};
+  const int rc = api.compile(prog, 3, opts);
+  size_t n = 0;
+  api.log_size(prog, &n);
+  log->assign(n, '\0');
+  if (n) api.log(prog, &(*log)[0]);
+  if (rc == 0) {
+    size_t cs = 0;
+    api.cubin_size(prog, &cs);
+    cubin->resize(cs);
+    api.cubin(prog, cubin->data());
+  }
+  api.destroy(&prog);
+  return rc == 0 ? SV_OK : SV_ERR_CUDA;
+}
+
+}  // namespace
+
+struct PassKernel {
+  cudaKernel_t kernel = nullptr;
+  int threads = 0, per_sm = 0;
+  size_t smem = 0;
+};
+
+struct Specialized {
+  std::vector<PassKernel> passes;  // indexed like the program's pass blocks
+};
+
+void specialized_free(Specialized* s) { delete s; }
+
+template <typename T>
+static int specialize_typed(Context* ctx, sv_program* prog) {
+  if (!nvrtc().ok)
+    return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
+  const int np = prog->npasses;
+  std::vector<std::string> names(np), sources(np);
+  for (int i = 0; i < np; i++) {
+    const PassParams<T>& p = *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)i * prog->pass_bytes);
+    names[i] = "sv_pass";
+    sources[i] = pass_source<T>(p, "sv_pass");
+    if (sources[i].empty()) return set_error(SV_ERR_UNSUPPORTED, "pass %d holds ops that cannot be specialised", i);
+  }
+  // compile the sources not in the cache, in parallel
+  std::vector<int> todo;
+  {
+    std::lock_guard<std::mutex> g(g_cache_mutex);
+    for (int i = 0; i < np; i++) {
+      if (cache().count(sources[i])) continue;
+      bool dup = false;
+      for (int j : todo) dup |= sources[j] == sources[i];
+      if (!dup) todo.push_back(i);
+    }
+  }
+  std::vector<std::vector<char>> cubins(todo.size());
+  std::vector<std::string> logs(todo.size());
+  std::vector<int> rcs(todo.size(), SV_OK);
+  {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthr = std::min<size_t>(todo.size(), hw);
+    std::vector<std::thread> pool;
+    std::mutex m;
+    size_t next = 0;
+    for (size_t w = 0; w < nthr; w++)
+      pool.emplace_back([&] {
+        for (;;) {
+          size_t k;
+          {
+            std::lock_guard<std::mutex> g(m);
+            if (next >= todo.size()) return;
+            k = next++;
+          }
+          rcs[k] = compile_cubin(sources[todo[k]], &cubins[k], &logs[k]);
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  for (size_t k = 0; k < todo.size(); k++)
+    if (rcs[k] != SV_OK)
+      return set_error(SV_ERR_CUDA, "runtime compilation of pass %d failed: %.400s", todo[k], logs[k].c_str());
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  {
+    std::lock_guard<std::mutex> g(g_cache_mutex);
+    for (size_t k = 0; k < todo.size(); k++) {
+      CompiledKernel ck;
+      SV_TRY(check_cuda(cudaLibraryLoadData(&ck.lib, cubins[k].data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+                        "cudaLibraryLoadData"));
+      SV_TRY(check_cuda(cudaLibraryGetKernel(&ck.kernel, ck.lib, names[todo[k]].c_str()), "cudaLibraryGetKernel"));
+      cache()[sources[todo[k]]] = ck;
+    }
+  }
+  std::unique_ptr<Specialized> s(new Specialized());
+  s->passes.resize(np);
+  const KernelShape ks = shape_of<T>(prog->kt);
+  for (int i = 0; i < np; i++) {
+    PassKernel& pk = s->passes[i];
+    {
+      std::lock_guard<std::mutex> g(g_cache_mutex);
+      pk.kernel = cache()[sources[i]].kernel;
+    }
+    pk.threads = ks.threads;
+    pk.smem = ks.smem;
+    SV_TRY(check_cuda(cudaKernelSetAttributeForDevice(pk.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)pk.smem, ctx->device),
+                      "specialised pass smem attribute"));
+    SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pk.per_sm, (const void*)pk.kernel, pk.threads,
+                                                                    pk.smem),
+                      "specialised pass occupancy"));
+    if (pk.per_sm < 1) return set_error(SV_ERR_ARG, "specialised pass %d does not fit on an SM", i);
+  }
+  if (prog->spec) specialized_free(prog->spec);
+  prog->spec = s.release();
+  return SV_OK;
+}
+
+int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state) {
+  const PassKernel& pk = prog->spec->passes[pass];
+  const unsigned char* block = prog->passes.data() + (size_t)pass * prog->pass_bytes;
+  const void* coef = prog->dtype == SV_C128 ? (const void*)reinterpret_cast<const PassParams<c128>*>(block)->coef
+                                            : (const void*)reinterpret_cast<const PassParams<c64>*>(block)->coef;
+  const int64_t ntiles = (int64_t)1 << (prog->nqubits - prog->kt);
+  int64_t grid = (int64_t)pk.per_sm * ctx->num_sms;
+  if (grid > ntiles) grid = ntiles;
+  void* args[] = {&state, const_cast<void*>(coef)};
+  SV_TRY(check_cuda(cudaLaunchKernel((const void*)pk.kernel, dim3((unsigned)grid), dim3(pk.threads), args, pk.smem,
+                                     ctx->stream),
+                    "specialised pass launch"));
+  return SV_OK;
+}
+
+}  // namespace sv
+
+extern "C" {
+
+int sv_program_specialize(sv_context* ctx, sv_program* prog) {
+  if (!ctx || !prog) return sv::set_error(SV_ERR_ARG, "null context or program");
+  return prog->dtype == SV_C128 ? sv::specialize_typed<sv::c128>(ctx, prog)
+                                : sv::specialize_typed<sv::c64>(ctx, prog);
+}
+
+}  // extern "C"

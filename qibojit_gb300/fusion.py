@@ -97,6 +97,15 @@ class FusedProgram:
         self._lib = lib
         self.ngates = len(ops)
         self._keep = None
+        self.specialized = False
+        self.runs = 0
+
+    def specialize(self) -> "FusedProgram":
+        """Compiles pass kernels with this program's structure as literals (the engine's
+        run-time specialiser, ``sv_program_specialize``); later runs launch them."""
+        _lib.check(self._lib.sv_program_specialize(self.ctx.handle, self._h), "sv_program_specialize")
+        self.specialized = True
+        return self
 
     def stats(self) -> dict:
         a, b, c, d = (ctypes.c_int() for _ in range(4))
@@ -114,6 +123,7 @@ class FusedProgram:
             raise ValueError("state must be a contiguous CUDA tensor")
         _lib.check(self._lib.sv_program_run(self.ctx.handle, self._h, ctypes.c_void_p(state.data_ptr())),
                    "sv_program_run")
+        self.runs += 1
         return state
 
     def close(self):
