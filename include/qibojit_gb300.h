@@ -154,6 +154,15 @@ int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* pr
                            int prob_dtype, int nbits, int64_t nshots, uint32_t seed,
                            int nchains);
 
+/* Direct sampling, the reference's branch below SHOT_METROPOLIS_THRESHOLD
+ * (cpu.py:384-385 -> qibo Backend.sample_shots = numpy.random.choice(N, nshots, p)):
+ * for each of the nshots uniforms in [0, 1) (host array, the caller's random_sample
+ * stream) the outcome is the first index whose FP64 cumulative probability exceeds
+ * u times the total.  `frequencies` (device int64, 2^nbits, added to) and `samples`
+ * (device int64, nshots) may each be NULL.  Synchronises the context's stream. */
+int sv_sample_cdf(sv_context* ctx, const void* probs, int prob_dtype, int nbits, const double* uniforms,
+                  int64_t nshots, int64_t* frequencies, int64_t* samples);
+
 /* -------------------------------------------------------------- reductions */
 /* The precision mode keeps bulk gate arithmetic in complex64 and every reduction in
  * FP64 (Neumaier-compensated per thread, fixed-order final sums).  These return

@@ -246,6 +246,17 @@ def mt_stream(seed: int, kind: str, count: int, high: int = 0) -> np.ndarray:
     return out
 
 
+def sample_shots(probs: np.ndarray, uniforms: np.ndarray) -> np.ndarray:
+    """Direct sampling as the reference's branch below SHOT_METROPOLIS_THRESHOLD
+    (``cpu.py:384-385``) reaches it: qibo's ``Backend.sample_shots`` is
+    ``numpy.random.choice(N, nshots, p=probs)``, whose legacy algorithm normalises
+    ``cdf = cumsum(p) / cdf[-1]`` in FP64, draws one ``random_sample`` per shot and
+    returns ``cdf.searchsorted(u, side="right")``.  The caller passes those uniforms."""
+    cdf = np.cumsum(np.asarray(probs, dtype=np.float64))
+    cdf /= cdf[-1]
+    return np.searchsorted(cdf, np.asarray(uniforms, dtype=np.float64), side="right").astype(np.int64)
+
+
 def probabilities(state: np.ndarray, qubits: Sequence[int], nqubits: int) -> np.ndarray:
     """|psi|^2 marginalised on ``qubits`` (qubit indices, qubits[0] most significant)."""
     dt = _check_state(state)

@@ -374,14 +374,42 @@ class GB300Backend(_QiboBackend):
             frequencies += work.to(frequencies.dtype)
         return frequencies
 
-    def sample_frequencies(self, probabilities, nshots: int) -> Counter:
-        seed = int(np.random.randint(0, int(1e8)))
+    def _sampling_probs(self, probabilities):
         probs = self.cast(probabilities, dtype=_dtype_name(getattr(probabilities, "dtype", "float64")))
         if _dtype_name(probs.dtype) not in ("float64", "float32"):
             probs = probs.real.contiguous()
+        nstates = int(probs.shape[0])
+        nbits = nstates.bit_length() - 1
+        if nstates != 1 << nbits:
+            raise ValueError("probabilities need 2^n entries")
+        return probs, _lib.DTYPE_CODES[_dtype_name(probs.dtype)], nbits
+
+    def sample_shots(self, probabilities, nshots: int):
+        """qibo's ``Backend.sample_shots``: ``numpy.random.choice(N, nshots, p=probabilities)``
+        with the global NumPy stream (one ``random_sample`` draw per shot, as NumPy's
+        choice takes them), each outcome searched on the device (``sv_sample_cdf``).
+        Returns the outcomes as an int64 CUDA tensor."""
         torch = _torch()
+        probs, pdt, nbits = self._sampling_probs(probabilities)
+        uniforms = np.ascontiguousarray(np.random.random_sample(int(nshots)), dtype=np.float64)
+        out = torch.empty(int(nshots), dtype=torch.int64, device=self._tdevice)
+        _lib.check(self.lib.sv_sample_cdf(self.ctx.handle, probs.data_ptr(), pdt, nbits, uniforms.ctypes.data,
+                                          int(nshots), None, out.data_ptr()), "sample_shots")
+        return out
+
+    def sample_frequencies(self, probabilities, nshots: int) -> Counter:
+        """cpu.py:383-394: below SHOT_METROPOLIS_THRESHOLD shots, direct sampling (qibo's
+        ``sample_shots`` path); from it on, the Metropolis chains of ``measure_frequencies``."""
+        torch = _torch()
+        probs, pdt, nbits = self._sampling_probs(probabilities)
         freqs = torch.zeros(probs.shape[0], dtype=torch.int64, device=self._tdevice)
-        freqs = self.measure_frequencies_op(freqs, probs, nshots, 0, seed, self.nthreads)
+        if nshots < SHOT_METROPOLIS_THRESHOLD:
+            uniforms = np.ascontiguousarray(np.random.random_sample(int(nshots)), dtype=np.float64)
+            _lib.check(self.lib.sv_sample_cdf(self.ctx.handle, probs.data_ptr(), pdt, nbits, uniforms.ctypes.data,
+                                              int(nshots), freqs.data_ptr(), None), "sample_frequencies")
+        else:
+            seed = int(np.random.randint(0, int(1e8)))
+            freqs = self.measure_frequencies_op(freqs, probs, nshots, 0, seed, self.nthreads)
         idx = torch.nonzero(freqs).flatten()
         return Counter(dict(zip(idx.cpu().tolist(), freqs[idx].cpu().tolist())))
 

@@ -533,11 +533,194 @@ static int sample_typed(Context* ctx, int64_t* freq, const void* probs, int nbit
   return SV_OK;
 }
 
+// ------------------------------------------------- direct sampling (inverse CDF)
+// Below qibo's SHOT_METROPOLIS_THRESHOLD the reference samples with qibo's
+// Backend.sample_shots, numpy.random.choice(N, nshots, p=probs) (the branch at
+// cpu.py:384-385): cdf = cumsum(p) / cdf[-1] in FP64 and, for each uniform u of the
+// global MT19937 stream (random_sample), the first index i with cdf[i] > u.  The
+// engine takes the same uniforms from the caller and searches an FP64 CDF built on
+// the device in two levels (sums of 4096-probability blocks, their prefix, then the
+// crossing inside one block), so the probabilities never leave the device.
+constexpr int kCdfBlock = 4096;                // probabilities per block
+constexpr int kCdfSeg = kCdfBlock / 32;        // per lane when a warp scans one block
+
+template <typename P>
+__global__ void __launch_bounds__(256) k_cdf_block_sums(const P* __restrict__ p, int64_t n, double* bsum) {
+  __shared__ double red[8];
+  const int64_t b0 = (int64_t)blockIdx.x * kCdfBlock;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < kCdfBlock; i += blockDim.x)
+    if (b0 + i < n) s += (double)p[b0 + i];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    bsum[blockIdx.x] = t;
+  }
+}
+
+// exclusive prefix of the block sums, bpre[nb] = total; one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) k_cdf_prefix(const double* bsum, int64_t nb, double* bpre) {
+  __shared__ double part[1024];
+  const int64_t per = (nb + 1023) / 1024;
+  const int64_t lo = threadIdx.x * per, hi = lo + per < nb ? lo + per : nb;
+  double s = 0.0;
+  for (int64_t i = lo; i < hi; i++) s += bsum[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {  // 1024 sequential adds: fixed order
+    double c = 0.0;
+    for (int t = 0; t < 1024; t++) {
+      const double x = part[t];
+      part[t] = c;
+      c += x;
+    }
+    bpre[nb] = c;
+  }
+  __syncthreads();
+  double c = part[threadIdx.x];
+  for (int64_t i = lo; i < hi; i++) {
+    bpre[i] = c;
+    c += bsum[i];
+  }
+}
+
+// largest index with a nonzero probability (the answer when u * total rounds up to total)
+template <typename P>
+__global__ void __launch_bounds__(256) k_last_nonzero(const P* __restrict__ p, int64_t n,
+                                                      unsigned long long* out) {
+  long long best = -1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (p[i] > (P)0) best = i;
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long o = __shfl_xor_sync(0xffffffffu, best, off);
+    best = o > best ? o : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best >= 0) atomicMax(out, (unsigned long long)best);
+}
+
+// one warp per shot: block by binary search over the prefix, then the lane segment whose
+// running sum crosses u * total, then the element inside it
+template <typename P>
+__global__ void __launch_bounds__(256) k_cdf_sample(const P* __restrict__ p, int64_t n, const double* __restrict__ bpre,
+                                                    int64_t nb, const double* __restrict__ u, int64_t nshots,
+                                                    const unsigned long long* last, unsigned long long* freq,
+                                                    int64_t* samples) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double total = bpre[nb];
+  for (int64_t shot = (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5); shot < nshots; shot += nwarps) {
+    const double t = u[shot] * total;
+    int64_t lo = 0, hi = nb - 1;  // last block whose prefix is <= t
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (bpre[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const int64_t e0 = lo * kCdfBlock + (int64_t)lane * kCdfSeg;
+    double seg = 0.0;
+    long long seglast = -1;  // last nonzero probability of this lane's segment
+    for (int i = 0; i < kCdfSeg; i++)
+      if (e0 + i < n) {
+        const double x = (double)p[e0 + i];
+        seg += x;
+        if (x > 0.0) seglast = e0 + i;
+      }
+    double inc = seg;  // inclusive warp scan of the segment sums
+    for (int off = 1; off < 32; off <<= 1) {
+      const double o = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += o;
+    }
+    const unsigned hit = __ballot_sync(0xffffffffu, bpre[lo] + inc > t);
+    long long idx = -1;
+    if (hit) {
+      const int L = __ffs(hit) - 1;
+      if (lane == L) {
+        double c = bpre[lo] + inc - seg;
+        long long lastpos = -1;
+        for (int i = 0; i < kCdfSeg && e0 + i < n; i++) {
+          const double x = (double)p[e0 + i];
+          if (x > 0.0) lastpos = e0 + i;
+          c += x;
+          if (c > t && x > 0.0) {
+            idx = e0 + i;
+            break;
+          }
+        }
+        if (idx < 0) idx = lastpos;  // rounding between the two running sums
+      }
+      idx = __shfl_sync(0xffffffffu, idx, L);
+    }
+    if (idx < 0) {
+      // no crossing inside the block: u * total sits within rounding of the block's end
+      // (or of the total); the last nonzero probability of the block, else of the state
+      long long bl = seglast;
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long o = __shfl_xor_sync(0xffffffffu, bl, off);
+        bl = o > bl ? o : bl;
+      }
+      idx = bl >= 0 ? bl : (long long)*last;
+    }
+    if (lane == 0) {
+      if (freq) atomicAdd(&freq[idx], 1ull);
+      if (samples) samples[shot] = idx;
+    }
+  }
+}
+
+template <typename P>
+static int sample_cdf_typed(Context* ctx, const void* probs, int nbits, const double* uniforms, int64_t nshots,
+                            int64_t* freq, int64_t* samples) {
+  const int64_t n = (int64_t)1 << nbits;
+  const int64_t nb = (n + kCdfBlock - 1) / kCdfBlock;
+  const size_t a = ((sizeof(double) * (size_t)nb + 255) / 256) * 256;
+  const size_t b = ((sizeof(double) * (size_t)(nb + 1) + 255) / 256) * 256;
+  const size_t c = ((sizeof(double) * (size_t)nshots + 255) / 256) * 256;
+  SV_TRY(ensure_scratch(ctx, a + b + c + 256));
+  unsigned char* base = (unsigned char*)ctx->scratch;
+  double* bsum = (double*)base;
+  double* bpre = (double*)(base + a);
+  double* du = (double*)(base + a + b);
+  unsigned long long* last = (unsigned long long*)(base + a + b + c);
+  SV_TRY(check_cuda(cudaMemcpyAsync(du, uniforms, sizeof(double) * nshots, cudaMemcpyHostToDevice, ctx->stream),
+                    "uniforms upload"));
+  SV_TRY(check_cuda(cudaMemsetAsync(last, 0, sizeof(unsigned long long), ctx->stream), "last index"));
+  k_cdf_block_sums<P><<<(unsigned)nb, 256, 0, ctx->stream>>>((const P*)probs, n, bsum);
+  SV_LAUNCH_CHECK("cdf block sums launch");
+  k_cdf_prefix<<<1, 1024, 0, ctx->stream>>>(bsum, nb, bpre);
+  SV_LAUNCH_CHECK("cdf prefix launch");
+  k_last_nonzero<P><<<stream_grid(ctx, n), 256, 0, ctx->stream>>>((const P*)probs, n, last);
+  SV_LAUNCH_CHECK("last nonzero launch");
+  const int64_t warps = nshots < (int64_t)ctx->num_sms * 64 ? nshots : (int64_t)ctx->num_sms * 64;
+  k_cdf_sample<P><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, ctx->stream>>>(
+      (const P*)probs, n, bpre, nb, du, nshots, last, (unsigned long long*)freq, samples);
+  SV_LAUNCH_CHECK("cdf sample launch");
+  // the uniforms came from pageable host memory: finish before the caller may reuse it
+  SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "cdf sampling"));
+  return SV_OK;
+}
+
 }  // namespace sv
 
 using namespace sv;
 
 extern "C" {
+
+int sv_sample_cdf(sv_context* ctx, const void* probs, int prob_dtype, int nbits, const double* uniforms,
+                  int64_t nshots, int64_t* frequencies, int64_t* samples) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  if (!probs || (nshots > 0 && !uniforms)) return set_error(SV_ERR_ARG, "probs and uniforms are required");
+  if (nbits < 0 || nbits > 34) return set_error(SV_ERR_ARG, "nbits = %d out of range [0, 34]", nbits);
+  if (nshots < 0) return set_error(SV_ERR_ARG, "nshots must be >= 0");
+  if (nshots == 0) return SV_OK;
+  for (int64_t i = 0; i < nshots; i++)
+    if (!(uniforms[i] >= 0.0 && uniforms[i] < 1.0)) return set_error(SV_ERR_ARG, "uniforms must lie in [0, 1)");
+  if (prob_dtype == SV_F64) return sample_cdf_typed<double>(ctx, probs, nbits, uniforms, nshots, frequencies, samples);
+  if (prob_dtype == SV_F32) return sample_cdf_typed<float>(ctx, probs, nbits, uniforms, nshots, frequencies, samples);
+  return set_error(SV_ERR_ARG, "prob_dtype must be SV_F64 or SV_F32");
+}
 
 int sv_zero_state(sv_context* ctx, void* state, int dtype, int nqubits) {
   if (!ctx) return set_error(SV_ERR_ARG, "null context");

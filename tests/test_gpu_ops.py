@@ -165,3 +165,60 @@ def test_measure_frequencies_sparse_probabilities(backend, nonzero, nshots):
     for i, freq in frequencies.items():
         assert freq != 0
         assert i in nonzero
+
+
+def _sampling_probs(nbits, seed, pdt, zeros=0.3):
+    rng = np.random.default_rng(seed)
+    p = rng.random(2**nbits)
+    p[rng.random(2**nbits) < zeros] = 0
+    p = (p / p.sum()).astype(pdt)
+    return p / p.sum()
+
+
+@pytest.mark.parametrize("pdt", ["float64", "float32"])
+@pytest.mark.parametrize("nbits,nshots,seed", [(1, 10, 1), (5, 1000, 2), (12, 20000, 3), (20, 99999, 4)])
+def test_sample_shots_is_numpy_choice(backend, nbits, nshots, seed, pdt):
+    """Below SHOT_METROPOLIS_THRESHOLD the reference samples with numpy.random.choice
+    (cpu.py:384-385 -> qibo sample_shots): same global-stream draws, same outcomes."""
+    p = _sampling_probs(nbits, seed, pdt)
+    np.random.seed(seed)
+    want = np.random.choice(range(len(p)), size=nshots, p=p)
+    np.random.seed(seed)
+    got = backend.to_numpy(backend.sample_shots(backend.cast(p, dtype=pdt), nshots))
+    np.testing.assert_array_equal(got, want)
+
+
+def test_sample_frequencies_below_threshold_match_numpy(backend):
+    from collections import Counter
+
+    p = _sampling_probs(14, 5, "float64")
+    np.random.seed(77)
+    want = Counter(np.random.choice(range(len(p)), size=50000, p=p).tolist())
+    np.random.seed(77)
+    got = backend.sample_frequencies(backend.cast(p, dtype="float64"), 50000)
+    assert got == want
+
+
+def test_sample_shots_large_state_vs_oracle(backend):
+    """2^26 outcomes (CDF over 16384 blocks): against the oracle's FP64 cumsum search.
+    The two cumulative sums round differently, so an outcome may move across a bin
+    boundary only when its uniform lies within ~1e-12 of it: none expected."""
+    n = 26
+    p = _sampling_probs(n, 6, "float32", zeros=0.5)
+    u = np.random.default_rng(7).random(100000)
+    want = O.sample_shots(p, u)
+    d = backend.cast(p, dtype="float32")
+    import ctypes
+
+    from qibojit_gb300 import _lib
+
+    torch = pytest.importorskip("torch")
+    out = torch.empty(len(u), dtype=torch.int64, device="cuda")
+    freqs = torch.zeros(2**n, dtype=torch.int64, device="cuda")
+    _lib.check(backend.lib.sv_sample_cdf(backend.ctx.handle, d.data_ptr(), _lib.SV_F32, n,
+                                         u.ctypes.data_as(ctypes.c_void_p), len(u), freqs.data_ptr(), out.data_ptr()))
+    got = out.cpu().numpy()
+    assert np.count_nonzero(got != want) <= 1
+    assert np.all(p[got] > 0)
+    assert int(freqs.sum()) == len(u)
+    np.testing.assert_array_equal(np.bincount(got, minlength=2**n), freqs.cpu().numpy())

@@ -147,3 +147,21 @@ def test_probabilities_semantics():
         kept = [i for i in range(n) if i in qubits]
         p = np.transpose(p, [kept.index(q) for q in qubits]).ravel()
         np.testing.assert_allclose(O.probabilities(x, qubits, n), p, atol=1e-15)
+
+
+@pytest.mark.parametrize("nbits,nshots,seed,pdt", [(3, 50, 1, "float64"), (10, 999, 2, "float64"),
+                                                   (12, 5000, 3, "float32"), (16, 99999, 4, "float64")])
+def test_sample_shots_restatement_is_numpy_choice(nbits, nshots, seed, pdt):
+    """The direct-sampling oracle reproduces numpy.random.choice(N, nshots, p) (qibo's
+    sample_shots) draw for draw from the same global-stream uniforms, zeros included."""
+    rng = np.random.default_rng(seed)
+    p = rng.random(2**nbits)
+    p[rng.random(2**nbits) < 0.3] = 0
+    p = (p / p.sum()).astype(pdt)
+    p = p / p.sum()
+    np.random.seed(seed)
+    want = np.random.choice(range(len(p)), size=nshots, p=p)
+    np.random.seed(seed)
+    got = O.sample_shots(p, np.random.random_sample(nshots))
+    np.testing.assert_array_equal(got, want)
+    assert np.all(p[got] > 0)
