@@ -307,6 +307,7 @@ def run_engine(args):
             "c128_plain_gates_per_s": ngates / (plain_ms["complex128"] / 1000.0),
             "precision": {
                 "infidelity_c64_vs_c128": 1.0 - abs(ip) ** 2,
+                "infidelity_normalised": 1.0 - abs(ip) ** 2 / (backend.norm2(s64, n) * backend.norm2(s128, n)),
                 "max_abs_err_c64_vs_c128": backend.max_abs_diff(s64, s128, n),
                 "norm2_fp64_c64": backend.norm2(s64, n),
                 "zz01_c64": backend.expectation_z(s64, [0, 1], n),
@@ -478,6 +479,58 @@ def _extra_workloads(torch, backend, stream, args):
     return out
 
 
+def run_precision(args):
+    """The precision configuration: brickwork n=32, depth 40 (1280 U3 + 620 CZ), the
+    complex64 state (32 GiB) on specialised fused passes against the complex128 state
+    (64 GiB) on fused passes, both on this GPU; the complex128 run is the reference
+    precision (its passes are pinned to the oracle at n <= 30 by the tests)."""
+    import torch
+
+    from qibojit_gb300 import MetaBackend, circuits
+
+    n, depth = args.precision_nqubits, 40
+    backend = MetaBackend.load("gb300")
+    circ = circuits.brickwork(n, depth, SEED)
+    ngates = len(circ.queue)
+    stream = torch.cuda.current_stream()
+    out = {}
+    states = {}
+    for dt, spec in (("complex64", True), ("complex128", False)):
+        t0 = time.perf_counter()
+        prog = backend.compile(circ, dt, specialize=spec)
+        plan_s = time.perf_counter() - t0
+        s = backend.zero_state(n, dtype=dt)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prog.run(s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[dt] = {"gates_per_s": ngates / (ms / 1000.0), "ms": ms, "passes": prog.stats()["passes"],
+                   "tile_bits": prog.stats()["tile_bits"], "plan_and_compile_s": round(plan_s, 2),
+                   "pass_kernels": "specialised" if spec else "interpreting"}
+        states[dt] = s
+        del prog
+    s64, s128 = states["complex64"], states["complex128"]
+    ip = backend.inner_product(s128, s64, n)
+    line = {
+        "metric": f"precision (brickwork n={n} depth {depth})", "n_gpus": 1, "dtype": "c64 vs c128",
+        "data": "synthetic", "config": {"workload": f"brickwork n={n} depth {depth} (seed {SEED})",
+                                        "gates": ngates, "state_bytes": {"c64": 8 << n, "c128": 16 << n}},
+        # 1 - |<psi128|psi64>|^2 (raw: includes the complex64 state's norm drift) and
+        # the infidelity of the normalised states
+        "infidelity_c64_vs_c128": 1.0 - abs(ip) ** 2,
+        "infidelity_normalised": 1.0 - abs(ip) ** 2 / (backend.norm2(s64, n) * backend.norm2(s128, n)),
+        "max_abs_err_c64_vs_c128": backend.max_abs_diff(s64, s128, n),
+        "norm2_fp64_c64": backend.norm2(s64, n),
+        "norm2_fp64_c128": backend.norm2(s128, n),
+        "zz01_c64": backend.expectation_z(s64, [0, 1], n),
+        "zz01_c128": backend.expectation_z(s128, [0, 1], n),
+        "runs": out,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -488,8 +541,13 @@ def main():
     ap.add_argument("--dtype", default="complex64", choices=["complex128", "complex64"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the variants and the precision report")
+    ap.add_argument("--precision", action="store_true",
+                    help="run only the precision configuration (brickwork depth 40, c64 against c128)")
+    ap.add_argument("--precision-nqubits", type=int, default=32)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.precision:
+        run_precision(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_engine(args)
