@@ -205,12 +205,16 @@ typedef struct sv_program sv_program;
 
 /* Plans and uploads a program for states of `nqubits` qubits and type `dtype`
  * (SV_C128 or SV_C64).  tile_bits <= 0 picks the default (11 for complex128, 12 for
- * complex64).  The op list is read before the call returns. */
+ * complex64).  The op list is read before the call returns.  The planner writes each
+ * uncontrolled one-qubit gate as diag * real 2x2 * diag and carries the diagonals to
+ * the next gate on their qubit (they commute with every diagonal gate), folding those
+ * of a phase into one table: the same unitary with fewer multiply-adds. */
 int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op* ops, int nops,
                        int tile_bits, sv_program** out);
 /* Applies the program to `state` (device, 2^nqubits amplitudes) on the context's stream. */
 int sv_program_run(sv_context* ctx, const sv_program* prog, void* state);
-/* Plan statistics: HBM passes, unfused ops, gates inside passes, tile bits (any may be NULL). */
+/* Plan statistics: HBM passes, unfused ops, planned ops inside passes (after one-qubit
+ * gate merging and phase folding), tile bits (any may be NULL). */
 int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* nfused_gates,
                      int* tile_bits);
 int sv_program_destroy(sv_program* prog);

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <complex>
 #include <vector>
 
 #include "sv_plan.cuh"
@@ -205,6 +206,30 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
           }
           continue;
         }
+        if (type == FOP_D1RUNR) {
+          if (pending_neg) {
+            apply_negations(v, pending_neg);
+            pending_neg = 0;
+          }
+          const int nr = op.nrun;
+          const T* c = cbase + op.coef;
+          if (nr == 4) {
+            dense1r_regs<T, 0>(v, c, 0xffffu);
+            dense1r_regs<T, 1>(v, c + 4, 0xffffu);
+            dense1r_regs<T, 2>(v, c + 8, 0xffffu);
+            dense1r_regs<T, 3>(v, c + 12, 0xffffu);
+          } else {
+#pragma unroll 1
+            for (int k = 0; k < nr; k++) dense1r_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+          }
+          continue;
+        }
+        if (type == FOP_DIAGR) {  // commutes with the pending sign flips
+          const T* c = cbase + op.coef;
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] = tmul(c[j], v[j]);
+          continue;
+        }
         const int flags = op.flags;
         if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
         if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;
@@ -349,6 +374,95 @@ static void merge_signs(FOp* ops, int begin, int* end) {
   *end = w;
 }
 
+// Folds runs of register-only diagonals of a phase (one-bit diagonals on register
+// slots, sign diagonals without thread or tile bits) into one FOP_DIAGR table of 16
+// complex factors, one multiply per amplitude for the whole run.  One-bit register
+// diagonals are first moved ahead of the mixing ops on other slots just before them
+// (they commute), which gathers the diagonals that a layer of one-qubit gates leaves
+// in front of it.  Table entries are products of the ops' FP64 entries.
+template <typename T>
+static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, int begin, int* end, int* ncoef,
+                                    int* slack, std::vector<int32_t>* src) {
+  auto diag_slot = [](const FOp& f) -> int {  // register slot of a one-bit register diagonal, else -1
+    if (f.type != FOP_DIAG || f.nd != 1 || f.omask || f.tmask || f.jmask != 0xffffu || f.tb[0] >= 0 || f.ob[0] >= 0)
+      return -1;
+    for (int u = 0; u < kRB; u++) {
+      bool same = true;
+      for (int j = 0; j < 16; j++)
+        if ((int)((f.rpart >> (4 * j)) & 15) != ((j >> u) & 1)) same = false;
+      if (same) return u;
+    }
+    return -1;
+  };
+  auto reg_sign = [](const FOp& f) {
+    if (f.type != FOP_SIGN || f.omask || f.tmask) return false;
+    for (int i = 0; i < f.nd; i++)
+      if (f.tb[i] >= 0 || f.ob[i] >= 0) return false;
+    return true;
+  };
+  for (int r = begin + 1; r < *end; r++) {
+    const int u = diag_slot(pp->ops[r]);
+    if (u < 0) continue;
+    const FOp f = pp->ops[r];
+    int q = r;
+    while (q > begin) {
+      const FOp& g = pp->ops[q - 1];
+      const bool two = g.type == FOP_DENSE2 || g.type == FOP_SWAP2;
+      const bool mixing = two || g.type == FOP_DENSE1 || g.type == FOP_DENSE1R || g.type == FOP_X1;
+      if (!mixing || g.u0 == u || (two && g.u1 == u)) break;  // controls on slot u commute with it
+      pp->ops[q] = g;
+      q--;
+    }
+    pp->ops[q] = f;
+  }
+  int w = begin;
+  for (int r = begin; r < *end;) {
+    if (diag_slot(pp->ops[r]) < 0 && !reg_sign(pp->ops[r])) {
+      pp->ops[w++] = pp->ops[r++];
+      continue;
+    }
+    int e = r, ndiag = 0;
+    while (e < *end && (diag_slot(pp->ops[e]) >= 0 || reg_sign(pp->ops[e]))) ndiag += diag_slot(pp->ops[e++]) >= 0;
+    if (ndiag == 0 || e - r < 2 || *slack < 16) {
+      while (r < e) pp->ops[w++] = pp->ops[r++];
+      continue;
+    }
+    std::complex<double> tab[16];
+    for (int j = 0; j < 16; j++) tab[j] = 1.0;
+    for (int q = r; q < e; q++) {
+      const FOp& f = pp->ops[q];
+      const int u = diag_slot(f);
+      if (u < 0) {
+        for (int j = 0; j < 16; j++)
+          if ((f.neg[0] >> j) & 1) tab[j] = -tab[j];
+        continue;
+      }
+      std::complex<double> c[2];
+      for (int b = 0; b < 2; b++) {
+        const HostOp& h = prog->ops[(*src)[2 * (f.coef + b)]];
+        const int ent = (*src)[2 * (f.coef + b) + 1];
+        c[b] = std::complex<double>(h.m[2 * ent], h.m[2 * ent + 1]);
+      }
+      for (int j = 0; j < 16; j++) tab[j] *= c[(j >> u) & 1];
+    }
+    FOp m;
+    memset(&m, 0, sizeof(m));
+    m.type = FOP_DIAGR;
+    m.jmask = 0xffffu;
+    m.coef = (uint32_t)*ncoef;
+    for (int j = 0; j < 16; j++) {
+      const double re_im[2] = {tab[j].real(), tab[j].imag()};
+      pp->coef[(*ncoef)++] = to_elem<T>(re_im);
+      src->push_back(-1);  // a product of several ops' entries: not refillable per circuit
+      src->push_back(j);
+    }
+    *slack -= 16;
+    pp->ops[w++] = m;
+    r = e;
+  }
+  *end = w;
+}
+
 template <typename T>
 static void encode_pass(const sv_program* prog, const std::vector<int>& sched, uint64_t S, PassParams<T>* pp,
                         int* nphases_out, std::vector<int32_t>* src) {
@@ -378,22 +492,34 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
     cur.clear();
     cur_bits.clear();
   };
+  // diagonal ops wait for the next dense op and join its phase: a diagonal emitted just
+  // before a gate on its qubit then finds that qubit in the registers
+  std::vector<Pending> held;
   for (int oi : sched) {
     const HostOp& h = prog->ops[oi];
     Pending pd{oi, {-1, -1}};
-    if (dense_like(h)) {
-      for (int i = 0; i < h.nt; i++) pd.lt[i] = local_of[h.tpos[i]];
-      int need = 0;
-      for (int i = 0; i < h.nt; i++)
-        if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) need++;
-      if ((int)cur_bits.size() + need > kRB) flush();
-      for (int i = 0; i < h.nt; i++)
-        if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) cur_bits.push_back(pd.lt[i]);
+    if (!dense_like(h)) {
+      held.push_back(pd);
+      continue;
     }
+    for (int i = 0; i < h.nt; i++) pd.lt[i] = local_of[h.tpos[i]];
+    int need = 0;
+    for (int i = 0; i < h.nt; i++)
+      if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) need++;
+    if ((int)cur_bits.size() + need > kRB) flush();
+    for (int i = 0; i < h.nt; i++)
+      if (std::find(cur_bits.begin(), cur_bits.end(), pd.lt[i]) == cur_bits.end()) cur_bits.push_back(pd.lt[i]);
+    cur.insert(cur.end(), held.begin(), held.end());
+    held.clear();
     cur.push_back(pd);
   }
+  cur.insert(cur.end(), held.begin(), held.end());
   flush();
   int nops = 0, ncoef = 0, ngrad = 0;
+  // coefficient slots left beyond those the scheduled ops need: room for the copies and
+  // tables that run merging and diagonal folding add
+  int slack = kCoefBytes / (int)sizeof(T);
+  for (int oi : sched) slack -= coef_cost(prog->ops[oi]);
   for (size_t g = 0; g < groups.size(); g++) {
     std::vector<int> rb = group_bits[g];
     for (int b = kt - 1; b >= 0 && (int)rb.size() < kRB; b--)
@@ -521,13 +647,15 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         }
       }
     }
+    if (prog->fold_diagonals) fold_register_diagonals<T>(prog, pp, P.op_begin, &nops, &ncoef, &slack, src);
     merge_signs(pp->ops, P.op_begin, &nops);
-    // merge runs of uncontrolled one-target dense ops into FOP_D1RUN records
+    // merge runs of uncontrolled one-target dense ops into FOP_D1RUN / FOP_D1RUNR records
     {
       int w = P.op_begin;
       for (int r = P.op_begin; r < nops;) {
         FOp f = pp->ops[r];
-        const bool plain1 = f.type == FOP_DENSE1 && f.omask == 0 && f.tmask == 0 && f.jmask == 0xffffu;
+        const bool plain1 = (f.type == FOP_DENSE1 || f.type == FOP_DENSE1R) && f.omask == 0 && f.tmask == 0 &&
+                            f.jmask == 0xffffu;
         if (!plain1) {
           pp->ops[w++] = f;
           r++;
@@ -535,39 +663,65 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         }
         FOp run;
         memset(&run, 0, sizeof(run));
-        run.type = FOP_D1RUN;
-        run.coef = f.coef;
+        run.type = f.type == FOP_DENSE1 ? FOP_D1RUN : FOP_D1RUNR;
         int k = 0;
         unsigned used = 0;
-        // coefficients of consecutive dense1 ops are contiguous (4 each, in emission order);
+        uint32_t gcoef[4];
+        bool contiguous = true;
         // a run holds gates on distinct register bits, which commute
         while (r < nops && k < 4) {
           const FOp& g2 = pp->ops[r];
-          const bool ok = g2.type == FOP_DENSE1 && g2.omask == 0 && g2.tmask == 0 && g2.jmask == 0xffffu &&
-                          g2.coef == run.coef + 4u * (unsigned)k && !((used >> g2.u0) & 1u);
+          const bool ok = g2.type == f.type && g2.omask == 0 && g2.tmask == 0 && g2.jmask == 0xffffu &&
+                          !((used >> g2.u0) & 1u);
           if (!ok) break;
           used |= 1u << g2.u0;
+          gcoef[k] = g2.coef;
+          contiguous &= g2.coef == f.coef + 4u * (unsigned)k;
           run.ru[k++] = g2.u0;
           r++;
         }
         run.nrun = (uint8_t)k;
-        if (k == 4) {
-          // reorder the four (commuting) gates and their matrices into register order 0..3
+        // the run's matrices back to back (four entries each): in place when the gates'
+        // coefficients already are, else copied to the end of the pass's array; four
+        // gates are sorted into register order 0..3
+        const bool sort4 = k == 4;
+        if (contiguous && !sort4) {
+          run.coef = f.coef;
+        } else if (!contiguous && slack < 4 * k) {
+          // no room for a copy: leave the gates as single-gate runs in place
+          for (int q = 0; q < k; q++) {
+            FOp one = run;
+            one.nrun = 1;
+            one.ru[0] = run.ru[q];
+            one.coef = gcoef[q];
+            pp->ops[w++] = one;
+          }
+          continue;
+        } else {
           T tmp[16];
           int32_t tsrc[32];
-          for (int q = 0; q < 4; q++)
+          for (int q = 0; q < k; q++) {
+            const int to_gate = sort4 ? run.ru[q] : q;
             for (int e = 0; e < 4; e++) {
-              const int from = run.coef + 4 * q + e, to = 4 * run.ru[q] + e;
+              const int from = (int)gcoef[q] + e, to = 4 * to_gate + e;
               tmp[to] = pp->coef[from];
               tsrc[2 * to] = (*src)[2 * from];
               tsrc[2 * to + 1] = (*src)[2 * from + 1];
             }
-          for (int e = 0; e < 16; e++) {
+          }
+          run.coef = contiguous ? f.coef : (uint32_t)ncoef;
+          if (!contiguous) {
+            ncoef += 4 * k;
+            slack -= 4 * k;
+            src->resize(2 * (size_t)ncoef);
+          }
+          for (int e = 0; e < 4 * k; e++) {
             pp->coef[run.coef + e] = tmp[e];
             (*src)[2 * (run.coef + e)] = tsrc[2 * e];
             (*src)[2 * (run.coef + e) + 1] = tsrc[2 * e + 1];
           }
-          for (int q = 0; q < 4; q++) run.ru[q] = (uint8_t)q;
+          if (sort4)
+            for (int q = 0; q < 4; q++) run.ru[q] = (uint8_t)q;
         }
         pp->ops[w++] = run;
       }
@@ -588,7 +742,12 @@ template <typename T>
 static int build_program(sv_program* prog) {
   const int n = prog->nqubits;
   const int kt = prog->kt;
-  const int coef_cap = kCoefBytes / (int)sizeof(T);
+  // folded programs leave a quarter of the coefficient slots for the encoder's run copies
+  // and register-diagonal tables (about 24 slots per phase)
+  const int coef_cap = (kCoefBytes / (int)sizeof(T)) * (prog->fold_diagonals ? 3 : 4) / 4;
+  // folded programs encode more, smaller ops; the adjoint sweep keeps one shared-memory
+  // gradient slot per op of a pass, so refilled programs stay at the smaller bound
+  const int max_ops = prog->fold_diagonals ? kMaxPassOps : kMaxPassOpsRefill;
   prog->pass_bytes = sizeof(PassParams<T>);
   // split at unfusable ops (dense on more than 2 targets, diagonal on more than 3)
   std::vector<std::vector<int>> runs(1);
@@ -622,8 +781,8 @@ static int build_program(sv_program* prog) {
         bits = tbits;
         for (int i = 0; i < h.nc; i++) bits |= 1ull << h.cpos[i];
         const int cc = coef_cost(h);
-        if (full || (bits & blocked) || nops + 1 > kMaxPassOps || ncoef + cc > coef_cap) {
-          if (nops + 1 > kMaxPassOps || ncoef + cc > coef_cap) full = true;
+        if (full || (bits & blocked) || nops + 1 > max_ops || ncoef + cc > coef_cap) {
+          if (nops + 1 > max_ops || ncoef + cc > coef_cap) full = true;
           blocked |= bits;
           next.push_back(oi);
           continue;
@@ -840,6 +999,98 @@ static void merge_single_qubit(std::vector<HostOp>& ops, int nqubits) {
   ops.swap(out);
 }
 
+// Phase folding (programs run through sv_program_create only).  Every uncontrolled
+// one-qubit gate with complex entries is written as D1 R D2: two diagonal phases and a
+// real 2x2 (a unitary 2x2 always separates so: |U_ij| e^{i(a_i + b_j)} up to signs).
+// A real 2x2 costs half the multiply-adds of a complex one, and the diagonals of all
+// gates commute with every diagonal gate (CZ, CU1, ...) and with gates on other qubits,
+// so they are carried along per qubit, multiplied together, and emitted only before
+// the next non-diagonal gate on their qubit.  For a layer of arbitrary one-qubit gates
+// between entangling diagonal layers this leaves one real 2x2 and one diagonal per
+// qubit and layer, and the encoder folds the diagonals of a phase's register bits into
+// one 16-entry table (FOP_DIAGR): about 5 instead of 8 FP multiply-adds per amplitude
+// and gate.
+static bool phase_separate(const HostOp& h, double d1[4], double r[4], double d2[4]) {
+  typedef std::complex<double> cd;
+  const cd a(h.m[0], h.m[1]), b(h.m[2], h.m[3]), c(h.m[4], h.m[5]), d(h.m[6], h.m[7]);
+  auto unit = [](cd z) { return std::abs(z) > 0 ? z / std::abs(z) : cd(1, 0); };
+  cd p0, p1, q0, q1;
+  if (std::abs(a) >= std::abs(b)) {
+    p0 = unit(a);
+    q0 = 1;
+    q1 = unit(b) / p0;
+  } else {
+    p0 = unit(b);
+    q1 = 1;
+    q0 = unit(a) / p0;
+  }
+  p1 = std::abs(c) >= std::abs(d) ? unit(c) / q0 : unit(d) / q1;
+  const cd m[4] = {a, b, c, d}, p[2] = {p0, p1}, q[2] = {q0, q1};
+  double err = 0;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) {
+      const cd rij = std::conj(p[i]) * m[2 * i + j] * std::conj(q[j]);
+      r[2 * i + j] = rij.real();
+      err = std::max(err, std::abs(p[i] * rij.real() * q[j] - m[2 * i + j]));
+    }
+  if (err > 1e-13) return false;
+  d1[0] = p0.real(), d1[1] = p0.imag(), d1[2] = p1.real(), d1[3] = p1.imag();
+  d2[0] = q0.real(), d2[1] = q0.imag(), d2[2] = q1.real(), d2[3] = q1.imag();
+  return true;
+}
+
+static void fold_phases(std::vector<HostOp>& ops) {
+  typedef std::complex<double> cd;
+  std::vector<HostOp> out;
+  std::vector<cd> pend0(64, cd(1, 0)), pend1(64, cd(1, 0));
+  std::vector<bool> pending(64, false);
+  auto flush = [&](int t) {
+    if (!pending[t]) return;
+    pending[t] = false;
+    const cd z0 = pend0[t], z1 = pend1[t];
+    pend0[t] = pend1[t] = cd(1, 0);
+    if (z0 == cd(1, 0) && z1 == cd(1, 0)) return;
+    HostOp g;
+    g.kind = SV_OP_DIAG;
+    g.nt = 1;
+    g.nc = 0;
+    g.tpos[0] = t;
+    g.m = {z0.real(), z0.imag(), z1.real(), z1.imag()};
+    classify(g);
+    out.push_back(std::move(g));
+  };
+  auto absorb = [&](int t, const double* dg) {  // pending diagonal of bit t times diag(dg)
+    pend0[t] *= cd(dg[0], dg[1]);
+    pend1[t] *= cd(dg[2], dg[3]);
+    pending[t] = true;
+  };
+  for (HostOp& h : ops) {
+    const bool one = h.nt == 1 && h.nc == 0;
+    if (one && h.kind == SV_OP_DIAG) {
+      absorb(h.tpos[0], h.m.data());
+      continue;
+    }
+    double d1[4], r[4], d2[4];
+    if (one && h.kind == SV_OP_DENSE && !h.is_real && !h.is_x && phase_separate(h, d1, r, d2)) {
+      const int t = h.tpos[0];
+      absorb(t, d2);  // applied first
+      flush(t);
+      HostOp g = h;
+      g.m = {r[0], 0.0, r[1], 0.0, r[2], 0.0, r[3], 0.0};
+      classify(g);
+      out.push_back(std::move(g));
+      absorb(t, d1);
+      continue;
+    }
+    // diagonal gates commute with the pending diagonals; other gates meet them on their targets
+    if (h.kind != SV_OP_DIAG)
+      for (int i = 0; i < h.nt; i++) flush(h.tpos[i]);
+    out.push_back(h);
+  }
+  for (int t = 0; t < 64; t++) flush(t);
+  ops.swap(out);
+}
+
 static int parse_ops(int nqubits, const sv_gate_op* ops, int nops, std::vector<HostOp>* out) {
   out->clear();
   for (int i = 0; i < nops; i++) {
@@ -880,9 +1131,11 @@ static int check_tile_bits(int dtype, int nqubits, int tile_bits, int* kt_out) {
   return SV_OK;
 }
 
-static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out) {
+static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out,
+                bool fold_diagonals = false) {
   if (kt > nqubits || kt < kLowBits + kRB) return set_error(SV_ERR_ARG, "tile of %d bits for %d qubits", kt, nqubits);
   sv_program* prog = new sv_program();
+  prog->fold_diagonals = fold_diagonals;
   prog->dtype = dtype;
   prog->nqubits = nqubits;
   prog->kt = kt;
@@ -894,6 +1147,19 @@ static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_pr
   }
   *out = prog;
   return SV_OK;
+}
+
+int refold_program(sv_program* prog) {
+  if (prog->fold_diagonals) return SV_OK;
+  fold_phases(prog->ops);
+  prog->fold_diagonals = true;
+  prog->segments.clear();
+  prog->passes.clear();
+  prog->coef_src.clear();
+  prog->pass_coef_off.clear();
+  prog->coef_total = 0;
+  prog->npasses = prog->nunfused = prog->nfused_gates = prog->nphases = 0;
+  return prog->dtype == SV_C128 ? build_program<c128>(prog) : build_program<c64>(prog);
 }
 
 }  // namespace sv
@@ -911,10 +1177,15 @@ int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op*
     return set_error(SV_ERR_ARG, "fused programs need %d..%d qubits", kLowBits + kRB, kMaxQubits);
   if (nops < 0 || (nops > 0 && !ops)) return set_error(SV_ERR_ARG, "bad op list");
   int kt = 0;
-  SV_TRY(check_tile_bits(dtype, nqubits, tile_bits, &kt));
+  // complex128 passes are FP64-bound: phase folding (fewer multiply-adds) pays on the
+  // interpreting kernel, best on 2^12-amplitude tiles; complex64 programs are folded
+  // when their passes are specialised (the interpreter runs the unfolded plan faster)
+  const bool fold = dtype == SV_C128;
+  SV_TRY(check_tile_bits(dtype, nqubits, tile_bits > 0 ? tile_bits : (fold ? 12 : 0), &kt));
   std::vector<HostOp> hops;
   SV_TRY(parse_ops(nqubits, ops, nops, &hops));
-  return plan(dtype, nqubits, kt, std::move(hops), out);
+  if (fold) fold_phases(hops);
+  return plan(dtype, nqubits, kt, std::move(hops), out, fold);
 }
 
 int sv_program_run(sv_context* ctx, const sv_program* prog, void* state) {
@@ -1374,6 +1645,10 @@ struct AdjArgs {
   double* gpart;        // [circuit][parameter][gstride]
   int32_t ncirc, nparams, gstride, pad;
 };
+static_assert(kAdjMaxGrad >= kMaxPassOpsRefill, "one gradient slot per op of an adjoint pass");
+// kernel parameters are limited to 32764 bytes
+static_assert(sizeof(PassParams<c128>) + sizeof(AdjArgs<c128>) <= 32764, "adjoint pass parameters");
+static_assert(sizeof(PassParams<c128>) + sizeof(BatchArgs<c128>) + sizeof(void*) <= 32764, "pass parameters");
 
 // products in the state's own precision (FP32 for complex64, FP64 for complex128);
 // block and circuit sums are FP64
@@ -1532,13 +1807,18 @@ __global__ void __launch_bounds__(MAXT, MINB) k_adjoint_pass(const __grid_consta
           if (lane == 0) gacc[op.u1 * nwarps + warp] += (double)acc;
           continue;
         }
-        if (type == FOP_D1RUN) {
-          // uncontrolled complex 2x2 gates on distinct register bits (fixed gates of the circuit)
+        if (type == FOP_D1RUN || type == FOP_D1RUNR) {
+          // uncontrolled 2x2 gates on distinct register bits (complex, or real such as RY)
           const T* c = cbase + op.coef;
 #pragma unroll 1
           for (int k = 0; k < op.nrun; k++) {
-            dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
-            dense1_dispatch(w, c + 4 * k, op.ru[k], 0xffffu);
+            if (type == FOP_D1RUN) {
+              dense1_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+              dense1_dispatch(w, c + 4 * k, op.ru[k], 0xffffu);
+            } else {
+              dense1r_dispatch(v, c + 4 * k, op.ru[k], 0xffffu);
+              dense1r_dispatch(w, c + 4 * k, op.ru[k], 0xffffu);
+            }
           }
           continue;
         }

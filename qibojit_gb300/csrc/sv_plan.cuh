@@ -14,7 +14,8 @@ namespace sv {
 constexpr int kRB = 4;            // register bits per phase (16 amplitudes per thread)
 constexpr int kMaxTile = 14;      // tile bits
 constexpr int kLowBits = 4;       // lowest bits always in a tile (contiguous runs)
-constexpr int kMaxPassOps = 128;  // ops (and phases) per pass
+constexpr int kMaxPassOps = 192;  // ops (and phases) per pass: capacity of the pass parameters
+constexpr int kMaxPassOpsRefill = 128;  // ops per pass of programs refilled per circuit (batches, adjoint)
 constexpr int kCoefBytes = 12288; // coefficient bytes per pass
 
 enum : uint8_t {
@@ -28,7 +29,9 @@ enum : uint8_t {
   FOP_SWAP2 = 7,    // SWAP: exchange of |01> and |10>, no arithmetic
   FOP_GRADX = 8,    // adjoint sweep: Im<lambda|X_q|psi> on a register bit (coef = parameter index)
   FOP_GRADY = 9,    //                Im<lambda|Y_q|psi>
-  FOP_GRADZ = 10    //                Im<lambda|Z_q|psi>, any bit (diagonal)
+  FOP_GRADZ = 10,   //                Im<lambda|Z_q|psi>, any bit (diagonal)
+  FOP_DIAGR = 11,   // diagonal over the 4 register bits: amplitude j times coefficient j
+  FOP_D1RUNR = 12   // FOP_D1RUN of real 2x2 gates
 };
 // internal op kind of the adjoint planner: a gradient marker (no matrix)
 constexpr int OP_GRAD = 2;
@@ -112,6 +115,10 @@ struct sv_program {
   std::vector<size_t> pass_coef_off;
   size_t coef_total = 0;
   int npasses = 0, nunfused = 0, nfused_gates = 0, nphases = 0;
+  // the encoder may fold a phase's one-bit register diagonals into one FOP_DIAGR table;
+  // its coefficients are products of several ops' entries, so programs whose
+  // coefficients are refilled per circuit (batches, adjoint sweeps) keep this off
+  bool fold_diagonals = false;
   // pass kernels compiled for this program's structure (sv_program_specialize), or null
   sv::Specialized* spec = nullptr;
 };
@@ -126,6 +133,8 @@ inline size_t pass_smem(int kt) {
   return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
 }
 
+// re-plans a program with phase folding (sv_fused.cu) unless it already has it
+int refold_program(sv_program* prog);
 // launches pass `pass` of a specialised program on the context stream
 int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state);
 void specialized_free(Specialized* s);

@@ -96,7 +96,9 @@ std::string deposit_expr(const char* var, const std::vector<int>& pos, bool wide
 
 int coef_count(const FOp& f) {
   switch (f.type) {
-    case FOP_D1RUN: return (int)f.coef + 4 * f.nrun;
+    case FOP_D1RUN:
+    case FOP_D1RUNR: return (int)f.coef + 4 * f.nrun;
+    case FOP_DIAGR: return (int)f.coef + 16;
     case FOP_DENSE1:
     case FOP_DENSE1R: return (int)f.coef + 4;
     case FOP_DENSE2: return (int)f.coef + 16;
@@ -201,14 +203,14 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
     for (int q = P.op_begin; q < P.op_end; q++) {
       const FOp& f = p.ops[q];
       std::ostringstream c;
-      if (f.type != FOP_D1RUN) {
+      if (f.type != FOP_D1RUN && f.type != FOP_D1RUNR && f.type != FOP_DIAGR) {
         if (f.omask) c << "((base & " << (long long)f.omask << "ll) == " << (long long)f.omask << "ll)";
         if (f.tmask) c << (f.omask ? " && " : "") << "((lbase & " << f.tmask << ") == " << f.tmask << ")";
       }
       const std::string cond = c.str();
       const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
-      if (f.type == FOP_D1RUN || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R || f.type == FOP_X1 ||
-          f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
+      if (f.type == FOP_D1RUN || f.type == FOP_D1RUNR || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R ||
+          f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
         flush();
       // non-register part of a diagonal's table index
       std::ostringstream te;
@@ -224,6 +226,14 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
         case FOP_D1RUN:
           for (int k = 0; k < f.nrun; k++)
             o << "      sv::dense1_regs<T, " << (int)f.ru[k] << ">(v, cf.c + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+          break;
+        case FOP_D1RUNR:
+          for (int k = 0; k < f.nrun; k++)
+            o << "      sv::dense1r_regs<T, " << (int)f.ru[k] << ">(v, cf.c + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+          break;
+        case FOP_DIAGR:  // commutes with the pending sign flips
+          for (int j = 0; j < 16; j++)
+            o << "      v[" << j << "] = sv::tmul(cf.c[" << (f.coef + j) << "], v[" << j << "]);\n";
           break;
         case FOP_DENSE1:
           o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
@@ -333,6 +343,8 @@ template <typename T>
 static int specialize_typed(Context* ctx, sv_program* prog) {
   if (!nvrtc().ok)
     return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
+  // specialised passes run the phase-folded plan fastest (no op decoding to pay for)
+  SV_TRY(refold_program(prog));
   const int np = prog->npasses;
   std::vector<std::string> names(np), sources(np);
   for (int i = 0; i < np; i++) {

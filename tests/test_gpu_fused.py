@@ -57,8 +57,9 @@ def test_brickwork_fused_vs_oracle(backend, n, depth):
 def test_brickwork_plan_is_compact(backend):
     prog = backend.compile(circuits.brickwork(30, 20, 1234), "complex64")
     st = prog.stats()
-    # edge qubits skip a CZ every other layer: their consecutive U3s are merged into one op
-    assert st["unfused"] == 0 and 850 <= st["fused_gates"] < 890
+    # engine ops after planning (edge qubits' consecutive U3s merge into one op; a
+    # phase-folded plan writes each U3 as a real rotation plus carried diagonals)
+    assert st["unfused"] == 0 and 850 <= st["fused_gates"] < 2 * 890
     assert st["passes"] < 890 // 8
 
 
