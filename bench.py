@@ -228,9 +228,8 @@ def run_engine(args):
     ngates = len(circ.queue)
     n_u3 = sum(1 for g in circ.queue if type(g).__name__ == "U3")
     # the headline program: pass kernels specialised to this circuit's structure at run
-    # time (complex64; compiled once, outside the timed region); complex128 passes are
-    # FP64-bound and run on the interpreting tile kernel
-    specialize = dtype == "complex64"
+    # time (compiled once, outside the timed region)
+    specialize = True
     t_spec = time.perf_counter()
     prog = backend.compile(circ, dtype, specialize=specialize)
     t_spec = time.perf_counter() - t_spec
@@ -294,7 +293,7 @@ def run_engine(args):
         int_ms = _time_program(torch, pint, backend, sint, _lib.SV_C64, n, 2, stream)
         del pint, sint
         torch.cuda.empty_cache()
-        p128 = backend.compile(circ, "complex128")
+        p128 = backend.compile(circ, "complex128", specialize=True)
         s128 = backend.zero_state(n, dtype="complex128")
         f128_ms = _time_program(torch, p128, backend, s128, _lib.SV_C128, n, 1, stream)
         s64 = backend.cast(final64, dtype="complex64")
@@ -497,7 +496,7 @@ def run_precision(args):
     stream = torch.cuda.current_stream()
     out = {}
     states = {}
-    for dt, spec in (("complex64", True), ("complex128", False)):
+    for dt, spec in (("complex64", True), ("complex128", True)):
         t0 = time.perf_counter()
         prog = backend.compile(circ, dt, specialize=spec)
         plan_s = time.perf_counter() - t0

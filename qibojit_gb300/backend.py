@@ -97,10 +97,8 @@ class GB300Backend(_QiboBackend):
         self.tensor_types = (np.ndarray, torch.Tensor)
         self.supports_multigpu = False
         self.fusion = True
-        # execute_circuit specialises a cached complex64 program's pass kernels
-        # (sv_program_specialize) once it has run this many times; None keeps the
-        # interpreting tile kernel.  complex128 passes are FP64-bound: specialising them
-        # does not pay, so they stay interpreted.
+        # execute_circuit specialises a cached program's pass kernels (sv_program_specialize)
+        # once it has run this many times; None keeps the interpreting tile kernel
         self.specialize_after: Optional[int] = 2
         self._programs = {}
 
@@ -456,8 +454,7 @@ class GB300Backend(_QiboBackend):
             if prog is None:
                 prog = self.compile(circuit, dtype)
                 self._programs = {key: prog}
-            elif (not prog.specialized and self.specialize_after is not None and prog.runs >= self.specialize_after
-                  and dtype == "complex64"):
+            elif not prog.specialized and self.specialize_after is not None and prog.runs >= self.specialize_after:
                 # a program run repeatedly: re-plan on the larger tile and compile its passes
                 runs = prog.runs
                 prog = self.compile(circuit, dtype, specialize=True)

@@ -182,6 +182,35 @@ __device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m
   }
 }
 
+// real 2x2 with a unit entry in each row (the row scale folded into a diagonal):
+// out_i = v_unit + r_i * v_other, one multiply-add per component; FORM bit i is the
+// column of row i's unit entry
+template <typename T>
+__device__ __forceinline__ T axpy_real(typename real_of<T>::type r, T x, T y) {  // r * x + y
+  if constexpr (is_complex<T>::value) return T{fma(r, x.re, y.re), fma(r, x.im, y.im)};
+  else return fma(r, x, y);
+}
+template <typename T, int U, int FORM>
+__device__ __forceinline__ void pivot1_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {
+  typename real_of<T>::type r0, r1;
+  if constexpr (is_complex<T>::value) {
+    r0 = m[0].re;
+    r1 = m[1].re;
+  } else {
+    r0 = m[0];
+    r1 = m[1];
+  }
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    if (!((jm >> j) & 1u)) continue;
+    const int k = j | (1 << U);
+    const T x = v[j], y = v[k];
+    v[j] = (FORM & 1) ? axpy_real(r0, x, y) : axpy_real(r0, y, x);
+    v[k] = (FORM & 2) ? axpy_real(r1, x, y) : axpy_real(r1, y, x);
+  }
+}
+
 template <typename T, int U0, int U1>
 __device__ __forceinline__ void swap2_regs(T (&v)[16], unsigned jm) {
 #pragma unroll

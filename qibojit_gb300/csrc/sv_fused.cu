@@ -52,6 +52,15 @@ __device__ __forceinline__ void dense1_dispatch(T (&v)[16], const T* m, int u, u
 }
 
 template <typename T>
+__device__ __forceinline__ void pivot1_dispatch(T (&v)[16], const T* m, int u, int form, unsigned jm) {
+#define SV_P1(U, F) \
+  if (u == U && form == F) { pivot1_regs<T, U, F>(v, m, jm); return; }
+  SV_P1(0, 0) SV_P1(0, 1) SV_P1(0, 2) SV_P1(0, 3) SV_P1(1, 0) SV_P1(1, 1) SV_P1(1, 2) SV_P1(1, 3)
+  SV_P1(2, 0) SV_P1(2, 1) SV_P1(2, 2) SV_P1(2, 3) SV_P1(3, 0) SV_P1(3, 1) SV_P1(3, 2) SV_P1(3, 3)
+#undef SV_P1
+}
+
+template <typename T>
 __device__ __forceinline__ void x1_dispatch(T (&v)[16], int u, unsigned jm) {
   switch (u) {
     case 0: x1_regs<T, 0>(v, jm); break;
@@ -233,13 +242,15 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
         const int flags = op.flags;
         if ((flags & FLAG_OMASK) && ((base & (int64_t)op.omask) != (int64_t)op.omask)) continue;
         if ((flags & FLAG_TMASK) && (((unsigned)lbase & op.tmask) != op.tmask)) continue;
-        if (type == FOP_DENSE1 || type == FOP_DENSE1R || type == FOP_X1 || type == FOP_SWAP2) {
+        if (type == FOP_DENSE1 || type == FOP_DENSE1R || type == FOP_DENSE1P || type == FOP_X1 ||
+            type == FOP_SWAP2) {
           if (pending_neg) {
             apply_negations(v, pending_neg);
             pending_neg = 0;
           }
           if (type == FOP_DENSE1) dense1_dispatch(v, cbase + op.coef, op.u0, op.jmask);
           else if (type == FOP_DENSE1R) dense1r_dispatch(v, cbase + op.coef, op.u0, op.jmask);
+          else if (type == FOP_DENSE1P) pivot1_dispatch(v, cbase + op.coef, op.u0, op.u1, op.jmask);
           else if (type == FOP_X1) x1_dispatch(v, op.u0, op.jmask);
           else swap2_dispatch(v, op.u0, op.u1, op.jmask);
         } else if (type == FOP_DENSE2) {
@@ -298,6 +309,7 @@ static int coef_cost(const HostOp& h) {
   if (h.kind == OP_GRAD) return 0;
   if (h.kind == SV_OP_DENSE) {
     if (h.is_x || (h.nt == 2 && h.is_swap)) return 0;
+    if (h.nt == 1 && h.unit_cols >= 0) return 2;  // the two row ratios of a pivoted real 2x2
     return h.nt == 1 ? 4 : 16;
   }
   return h.sign_only ? 0 : (1 << h.nt);
@@ -408,7 +420,8 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
     while (q > begin) {
       const FOp& g = pp->ops[q - 1];
       const bool two = g.type == FOP_DENSE2 || g.type == FOP_SWAP2;
-      const bool mixing = two || g.type == FOP_DENSE1 || g.type == FOP_DENSE1R || g.type == FOP_X1;
+      const bool mixing = two || g.type == FOP_DENSE1 || g.type == FOP_DENSE1R || g.type == FOP_DENSE1P ||
+                          g.type == FOP_X1;
       if (!mixing || g.u0 == u || (two && g.u1 == u)) break;  // controls on slot u commute with it
       pp->ops[q] = g;
       q--;
@@ -580,8 +593,10 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         }
         f.rpart = rpart;
       } else if (h.kind == SV_OP_DENSE) {
-        if (h.nt == 1) f.type = h.is_x ? FOP_X1 : (h.is_real ? FOP_DENSE1R : FOP_DENSE1);
-        else f.type = h.is_swap ? FOP_SWAP2 : FOP_DENSE2;
+        if (h.nt == 1)
+          f.type = h.is_x ? FOP_X1 : (h.unit_cols >= 0 ? FOP_DENSE1P : (h.is_real ? FOP_DENSE1R : FOP_DENSE1));
+        else
+          f.type = h.is_swap ? FOP_SWAP2 : FOP_DENSE2;
         f.u0 = (uint8_t)regpos[pd.lt[0]];
         tbits = 1u << f.u0;
         if (h.nt == 2) {
@@ -593,11 +608,22 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
         if (reg_c == 0) jm = 0xffffu;  // no register-level controls: kernel skips the tests
         f.jmask = (uint16_t)jm;
         f.coef = (uint32_t)ncoef;
-        const int ne = coef_cost(h);
-        for (int i = 0; i < ne; i++) {
-          src->push_back(pd.op);
-          src->push_back(i);
-          pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+        if (f.type == FOP_DENSE1P) {
+          // coefficients: row i's ratio, the entry beside its unit
+          f.u1 = (uint8_t)h.unit_cols;
+          for (int i = 0; i < 2; i++) {
+            const int e = 2 * i + (((h.unit_cols >> i) & 1) ? 0 : 1);
+            src->push_back(pd.op);
+            src->push_back(e);
+            pp->coef[ncoef++] = to_elem<T>(&h.m[2 * e]);
+          }
+        } else {
+          const int ne = coef_cost(h);
+          for (int i = 0; i < ne; i++) {
+            src->push_back(pd.op);
+            src->push_back(i);
+            pp->coef[ncoef++] = to_elem<T>(&h.m[2 * i]);
+          }
         }
       } else {
         f.nd = (uint8_t)h.nt;
@@ -1071,12 +1097,44 @@ static void fold_phases(std::vector<HostOp>& ops) {
       continue;
     }
     double d1[4], r[4], d2[4];
-    if (one && h.kind == SV_OP_DENSE && !h.is_real && !h.is_x && phase_separate(h, d1, r, d2)) {
+    const bool real1 = one && h.kind == SV_OP_DENSE && h.is_real && !h.is_x;
+    if (real1) {  // already real: no phases to separate
+      for (int i = 0; i < 4; i++) r[i] = h.m[2 * i];
+      d1[0] = d1[2] = d2[0] = d2[2] = 1.0;
+      d1[1] = d1[3] = d2[1] = d2[3] = 0.0;
+    }
+    if (real1 || (one && h.kind == SV_OP_DENSE && !h.is_real && !h.is_x && phase_separate(h, d1, r, d2))) {
       const int t = h.tpos[0];
       absorb(t, d2);  // applied first
       flush(t);
+      // R = diag(p0, p1) P: each row divided by its larger entry (|ratio| <= 1), the row
+      // scales joining the diagonal that follows
+      double pm[4], piv[2];
+      int cols = 0;
+      bool ok = true;
+      for (int i = 0; i < 2 && ok; i++) {
+        const double a = r[2 * i], b = r[2 * i + 1];
+        if (a == 0.0 && b == 0.0) ok = false;
+        else if (std::fabs(a) >= std::fabs(b)) {
+          piv[i] = a;
+          pm[2 * i] = 1.0;
+          pm[2 * i + 1] = b / a;
+        } else {
+          piv[i] = b;
+          pm[2 * i] = a / b;
+          pm[2 * i + 1] = 1.0;
+          cols |= 1 << i;
+        }
+      }
       HostOp g = h;
-      g.m = {r[0], 0.0, r[1], 0.0, r[2], 0.0, r[3], 0.0};
+      if (ok) {
+        g.m = {pm[0], 0.0, pm[1], 0.0, pm[2], 0.0, pm[3], 0.0};
+        g.unit_cols = cols;
+        const double dp[4] = {d1[0] * piv[0], d1[1] * piv[0], d1[2] * piv[1], d1[3] * piv[1]};
+        for (int i = 0; i < 4; i++) d1[i] = dp[i];
+      } else {
+        g.m = {r[0], 0.0, r[1], 0.0, r[2], 0.0, r[3], 0.0};
+      }
       classify(g);
       out.push_back(std::move(g));
       absorb(t, d1);

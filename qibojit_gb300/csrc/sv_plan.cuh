@@ -31,7 +31,8 @@ enum : uint8_t {
   FOP_GRADY = 9,    //                Im<lambda|Y_q|psi>
   FOP_GRADZ = 10,   //                Im<lambda|Z_q|psi>, any bit (diagonal)
   FOP_DIAGR = 11,   // diagonal over the 4 register bits: amplitude j times coefficient j
-  FOP_D1RUNR = 12   // FOP_D1RUN of real 2x2 gates
+  FOP_D1RUNR = 12,  // FOP_D1RUN of real 2x2 gates
+  FOP_DENSE1P = 13  // real 2x2 with a unit entry in each row (u1 bit i: row i's unit is in column 1)
 };
 // internal op kind of the adjoint planner: a gradient marker (no matrix)
 constexpr int OP_GRAD = 2;
@@ -86,6 +87,7 @@ struct HostOp {
   bool is_x = false;        // dense one-target [[0, 1], [1, 0]]
   bool is_real = false;     // dense with all-real entries
   bool is_swap = false;     // dense two-target SWAP
+  int unit_cols = -1;       // pivoted real 2x2 (phase folding): bit i = column of row i's unit entry
   int gen = 0;              // OP_GRAD: generator 1 = X, 2 = Y, 3 = Z
   int param = -1;           // OP_GRAD: parameter index
 };

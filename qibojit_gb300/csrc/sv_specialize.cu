@@ -101,6 +101,7 @@ int coef_count(const FOp& f) {
     case FOP_DIAGR: return (int)f.coef + 16;
     case FOP_DENSE1:
     case FOP_DENSE1R: return (int)f.coef + 4;
+    case FOP_DENSE1P: return (int)f.coef + 2;
     case FOP_DENSE2: return (int)f.coef + 16;
     case FOP_DIAG: return (int)f.coef + (1 << f.nd);
     default: return 0;
@@ -210,7 +211,7 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
       const std::string cond = c.str();
       const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
       if (f.type == FOP_D1RUN || f.type == FOP_D1RUNR || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R ||
-          f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
+          f.type == FOP_DENSE1P || f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
         flush();
       // non-register part of a diagonal's table index
       std::ostringstream te;
@@ -237,6 +238,10 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
           break;
         case FOP_DENSE1:
           o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
+          break;
+        case FOP_DENSE1P:
+          o << pre << "sv::pivot1_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, cf.c + " << f.coef << ", "
+            << f.jmask << "u);\n";
           break;
         case FOP_DENSE1R:
           o << pre << "sv::dense1r_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";

@@ -74,11 +74,13 @@ def test_execute_circuit_specialises_repeated_programs(backend):
     prog = backend._programs[key]
     assert prog.specialized and prog.stats()["tile_bits"] == 13
     np.testing.assert_allclose(again, first, rtol=0, atol=PARITY_ATOL["complex64"])
-    # complex128 programs stay interpreted
+    # complex128 programs too, on the default tile
     y = random_state(n, 23)
-    for _ in range(backend.specialize_after + 1):
-        backend.execute_circuit(circ, y)
-    assert not backend._programs[next(iter(backend._programs))].specialized
+    first128 = backend.to_numpy(backend.execute_circuit(circ, y))
+    for _ in range(backend.specialize_after):
+        again128 = backend.to_numpy(backend.execute_circuit(circ, y))
+    assert backend._programs[next(iter(backend._programs))].specialized
+    np.testing.assert_allclose(again128, first128, rtol=0, atol=1e-13)
 
 
 @pytest.mark.parametrize("dt", ["complex64", "complex128"])
