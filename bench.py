@@ -375,7 +375,9 @@ def _extra_workloads(torch, backend, stream, args):
     xd = backend.cast(x)
     res = {}
     for mode in ("plain", "fused"):
-        s = backend.execute_circuit(q, xd, fuse=(mode == "fused"))
+        # warm-up past the program cache's specialisation point (compiled once, untimed)
+        for _ in range((backend.specialize_after or 0) + 1):
+            s = backend.execute_circuit(q, xd, fuse=(mode == "fused"))
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
