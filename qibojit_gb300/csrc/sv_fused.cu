@@ -476,6 +476,109 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
   *end = w;
 }
 
+// one op of a phase: its program index and the local tile bits of its dense targets
+struct Pending {
+  int op;
+  int lt[2];
+};
+
+// Phase packing for folded programs: ops are placed by their dependencies rather than
+// in program order.  An op depends on the earlier ops of the pass it does not commute
+// with (two diagonals commute; a diagonal and a dense op commute unless the dense op
+// targets one of the diagonal's bits; dense ops commute when they share no qubit).  A
+// phase takes its register bits from the first ready dense ops and then every ready
+// op whose dense targets fit them, in program order, so a block of qubits runs as many
+// layers as its light cone allows before the tile is exchanged.  One-qubit diagonals
+// wait for a phase holding their qubit in the registers (where they fold into the
+// phase's diagonal table) and join just before the first gate that needs them.
+static void pack_phases(const sv_program* prog, const std::vector<int>& sched, const int* local_of,
+                        std::vector<std::vector<Pending>>* groups, std::vector<std::vector<int>>* group_bits) {
+  const int m = (int)sched.size();
+  std::vector<uint64_t> tbits(m), allbits(m);
+  std::vector<char> diag(m), one_diag(m);
+  for (int i = 0; i < m; i++) {
+    const HostOp& h = prog->ops[sched[i]];
+    uint64_t t = 0, a = 0;
+    for (int k = 0; k < h.nt; k++) t |= 1ull << h.tpos[k];
+    a = t;
+    for (int k = 0; k < h.nc; k++) a |= 1ull << h.cpos[k];
+    tbits[i] = t;
+    allbits[i] = a;
+    diag[i] = !dense_like(h) && h.kind != OP_GRAD;
+    one_diag[i] = diag[i] && h.nt == 1 && h.nc == 0;
+  }
+  auto commute = [&](int i, int j) {
+    if (diag[i] && diag[j]) return true;
+    if (diag[i]) return (tbits[j] & allbits[i]) == 0;
+    if (diag[j]) return (tbits[i] & allbits[j]) == 0;
+    return (allbits[i] & allbits[j]) == 0;
+  };
+  std::vector<std::vector<int>> preds(m);
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < i; j++)
+      if (!commute(i, j)) preds[i].push_back(j);
+  std::vector<char> done(m, 0);
+  int left = m;
+  while (left > 0) {
+    std::vector<Pending> cur;
+    std::vector<int> bits;
+    auto ready = [&](int i) {
+      for (int j : preds[i])
+        if (!done[j]) return false;
+      return true;
+    };
+    auto place = [&](int i) {
+      Pending pd{sched[i], {-1, -1}};
+      const HostOp& h = prog->ops[sched[i]];
+      if (!diag[i])
+        for (int k = 0; k < h.nt; k++) pd.lt[k] = local_of[h.tpos[k]];
+      cur.push_back(pd);
+      done[i] = 1;
+      left--;
+    };
+    for (int i = 0; i < m; i++) {
+      if (done[i]) continue;
+      if (diag[i]) {
+        // a one-qubit diagonal waits for a phase with its qubit in the registers
+        if (one_diag[i]) {
+          const int lb = local_of[prog->ops[sched[i]].tpos[0]];
+          if (lb < 0 || std::find(bits.begin(), bits.end(), lb) == bits.end()) continue;
+        }
+        if (ready(i)) place(i);
+        continue;
+      }
+      // a dense op: its one-qubit diagonal predecessors on its own targets join first
+      bool ok = true;
+      for (int j : preds[i])
+        if (!done[j] && !(one_diag[j] && (tbits[j] & tbits[i]) && ready(j))) ok = false;
+      if (!ok) continue;
+      const HostOp& h = prog->ops[sched[i]];
+      std::vector<int> nb = bits;
+      for (int k = 0; k < h.nt; k++) {
+        const int lb = local_of[h.tpos[k]];
+        if (std::find(nb.begin(), nb.end(), lb) == nb.end()) nb.push_back(lb);
+      }
+      if ((int)nb.size() > kRB) continue;
+      bits = nb;
+      for (int j : preds[i])
+        if (!done[j]) place(j);
+      place(i);
+    }
+    if (cur.empty()) {
+      // only one-qubit diagonals whose qubit no later phase holds are left (they commute
+      // with each other): they join the last phase
+      for (int i = 0; i < m; i++)
+        if (!done[i]) place(i);
+      if (!groups->empty()) {
+        groups->back().insert(groups->back().end(), cur.begin(), cur.end());
+        continue;
+      }
+    }
+    groups->push_back(cur);
+    group_bits->push_back(bits);
+  }
+}
+
 template <typename T>
 static void encode_pass(const sv_program* prog, const std::vector<int>& sched, uint64_t S, PassParams<T>* pp,
                         int* nphases_out, std::vector<int32_t>* src) {
@@ -493,7 +596,6 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
     }
   }
   // group ops into phases by register bits (order preserved)
-  struct Pending { int op; int lt[2]; };
   std::vector<std::vector<Pending>> groups;
   std::vector<std::vector<int>> group_bits;
   std::vector<int> cur_bits;
@@ -505,6 +607,9 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
     cur.clear();
     cur_bits.clear();
   };
+  if (prog->fold_diagonals) {
+    pack_phases(prog, sched, local_of, &groups, &group_bits);
+  } else {
   // diagonal ops wait for the next dense op and join its phase: a diagonal emitted just
   // before a gate on its qubit then finds that qubit in the registers
   std::vector<Pending> held;
@@ -528,6 +633,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
   }
   cur.insert(cur.end(), held.begin(), held.end());
   flush();
+  }
   int nops = 0, ncoef = 0, ngrad = 0;
   // coefficient slots left beyond those the scheduled ops need: room for the copies and
   // tables that run merging and diagonal folding add
