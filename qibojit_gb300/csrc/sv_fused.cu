@@ -17,6 +17,14 @@
 // the kernel parameters (constant bank); tiles are double-buffered with cp.async so
 // the next tile's HBM read overlaps this tile's arithmetic.
 //
+// Programs can be phase-folded (fold_phases, fold_register_diagonals, pack_phases):
+// every one-qubit gate becomes diag * pivoted real 2x2 * diag, diagonals are carried
+// to the next gate on their qubit and folded per phase into one register table, and
+// phases are packed by dependency so a block of qubits runs several layers per tile
+// exchange.  Complex128 programs always fold; complex64 programs fold when their
+// passes are compiled into specialised kernels (sv_specialize.cu), because this
+// interpreting kernel pays a decode cost per op.
+//
 // This replaces the reference's fusion path (qibo Circuit.fuse -> FusedGate, applied
 // by qibojit as one dense 2^k x 2^k multi-qubit kernel, cpu.py:535-537,
 // gpu.py:929-930) with a schedule that needs no dense products of gate matrices.
