@@ -254,9 +254,9 @@ def run_engine(args):
     pass_ms = (ms_step - zs_ms) / st["passes"]
 
     # ---- end to end through the public API: pinned host -> device -> host every step
-    host_in = torch.zeros(1 << n, dtype=state.dtype).pin_memory()
+    host_in = backend.host_buffer(n, dtype)  # pinned, on the GPU's local memory node
     host_in[0] = 1
-    host_out = torch.empty_like(host_in).pin_memory()
+    host_out = backend.host_buffer(n, dtype)
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range((backend.specialize_after or 0) + 1):  # plans, caches and specialises the program
         backend.execute_circuit(circ, host_in)

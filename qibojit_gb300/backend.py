@@ -54,6 +54,26 @@ def _torch():
     return torch
 
 
+def _gpu_local_cpus(device: int):
+    """CPUs next to the GPU (its PCI device's local_cpulist), or None if unknown."""
+    torch = _torch()
+    try:
+        pr = torch.cuda.get_device_properties(device)
+        busid = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{busid}/local_cpulist") as f:
+            text = f.read().strip()
+    except (OSError, AttributeError, RuntimeError):
+        return None
+    cpus = set()
+    for part in text.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    return cpus & os.sched_getaffinity(0) or None
+
+
 def _torch_dtype(name: str):
     global _TORCH_DTYPES
     if _TORCH_DTYPES is None:
@@ -168,6 +188,26 @@ class GB300Backend(_QiboBackend):
         return np.ascontiguousarray(np.asarray(matrix, dtype=dtype).ravel())
 
     # -------------------------------------------------------------- state creation
+    def host_buffer(self, nqubits: int, dtype=None):
+        """A pinned host array of 2^nqubits amplitudes in memory next to the GPU.
+
+        Host<->device copies of a state run at the link rate only from the GPU's local
+        memory node; pinned pages are placed where the allocating thread runs, so the
+        allocation runs on the GPU's local CPUs (the process affinity is restored)."""
+        torch = _torch()
+        tdt = _torch_dtype(_dtype_name(dtype) if dtype is not None else self.dtype)
+        cpus = _gpu_local_cpus(self._tdevice.index or 0)
+        old = os.sched_getaffinity(0)
+        try:
+            if cpus:
+                os.sched_setaffinity(0, cpus)
+            buf = torch.empty(1 << int(nqubits), dtype=tdt, pin_memory=True)
+            buf.zero_()
+        finally:
+            if cpus:
+                os.sched_setaffinity(0, old)
+        return buf
+
     def zero_state(self, nqubits: int, density_matrix: bool = False, dtype=None):
         """|0...0> (or |0><0| as a 2^n x 2^n matrix, cpu.py:334-353)."""
         dtype = _dtype_name(dtype) if dtype is not None else self.dtype

@@ -17,13 +17,13 @@
 // the kernel parameters (constant bank); tiles are double-buffered with cp.async so
 // the next tile's HBM read overlaps this tile's arithmetic.
 //
-// Programs can be phase-folded (fold_phases, fold_register_diagonals, pack_phases):
-// every one-qubit gate becomes diag * pivoted real 2x2 * diag, diagonals are carried
-// to the next gate on their qubit and folded per phase into one register table, and
-// phases are packed by dependency so a block of qubits runs several layers per tile
-// exchange.  Complex128 programs always fold; complex64 programs fold when their
-// passes are compiled into specialised kernels (sv_specialize.cu), because this
-// interpreting kernel pays a decode cost per op.
+// Phases are packed by dependency (pack_phases), so a block of qubits runs several
+// layers per tile exchange.  Programs can also be phase-folded (fold_phases,
+// fold_register_diagonals): every one-qubit gate becomes diag * pivoted real 2x2 *
+// diag, and diagonals are carried to the next gate on their qubit and folded per phase
+// into one register table.  Complex128 programs always fold; complex64 programs fold
+// when their passes are compiled into specialised kernels (sv_specialize.cu), because
+// this interpreting kernel pays a decode cost per op.
 //
 // This replaces the reference's fusion path (qibo Circuit.fuse -> FusedGate, applied
 // by qibojit as one dense 2^k x 2^k multi-qubit kernel, cpu.py:535-537,
@@ -490,7 +490,7 @@ struct Pending {
   int lt[2];
 };
 
-// Phase packing for folded programs: ops are placed by their dependencies rather than
+// Phase packing: ops are placed by their dependencies rather than
 // in program order.  An op depends on the earlier ops of the pass it does not commute
 // with (two diagonals commute; a diagonal and a dense op commute unless the dense op
 // targets one of the diagonal's bits; dense ops commute when they share no qubit).  A
@@ -615,7 +615,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
     cur.clear();
     cur_bits.clear();
   };
-  if (prog->fold_diagonals) {
+  if (prog->pack_phases) {
     pack_phases(prog, sched, local_of, &groups, &group_bits);
   } else {
   // diagonal ops wait for the next dense op and join its phase: a diagonal emitted just
@@ -1304,10 +1304,11 @@ static int check_tile_bits(int dtype, int nqubits, int tile_bits, int* kt_out) {
 }
 
 static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out,
-                bool fold_diagonals = false) {
+                bool fold_diagonals = false, bool pack = true) {
   if (kt > nqubits || kt < kLowBits + kRB) return set_error(SV_ERR_ARG, "tile of %d bits for %d qubits", kt, nqubits);
   sv_program* prog = new sv_program();
   prog->fold_diagonals = fold_diagonals;
+  prog->pack_phases = pack;
   prog->dtype = dtype;
   prog->nqubits = nqubits;
   prog->kt = kt;
@@ -2398,8 +2399,8 @@ int sv_adjoint_create(sv_context* ctx, int dtype, int ncirc, int nqubits, const 
     int ktf = kt + 1;
     if (ktf > nqubits) ktf = nqubits;
     if (ktf > (dtype == SV_C128 ? 12 : 13)) ktf = kt;
-    rc = plan(dtype, nqubits, ktf, std::move(f0), &sg.fwd);
-    if (rc == SV_OK) rc = plan(dtype, nqubits, kt, std::move(bw0), &sg.bwd);
+    rc = plan(dtype, nqubits, ktf, std::move(f0), &sg.fwd, false, false);
+    if (rc == SV_OK) rc = plan(dtype, nqubits, kt, std::move(bw0), &sg.bwd, false, false);
     if (rc == SV_OK && (sg.fwd->nunfused || sg.bwd->nunfused))
       rc = set_error(SV_ERR_UNSUPPORTED, "adjoint circuits need gates on at most 2 targets");
     if (rc == SV_OK)

@@ -121,6 +121,10 @@ struct sv_program {
   // its coefficients are products of several ops' entries, so programs whose
   // coefficients are refilled per circuit (batches, adjoint sweeps) keep this off
   bool fold_diagonals = false;
+  // group a pass's ops into phases by dependency (several layers per tile exchange)
+  // rather than in program order; adjoint sweeps keep program order around their
+  // gradient markers
+  bool pack_phases = false;
   // pass kernels compiled for this program's structure (sv_program_specialize), or null
   sv::Specialized* spec = nullptr;
 };

@@ -222,3 +222,11 @@ def test_sample_shots_large_state_vs_oracle(backend):
     assert np.all(p[got] > 0)
     assert int(freqs.sum()) == len(u)
     np.testing.assert_array_equal(np.bincount(got, minlength=2**n), freqs.cpu().numpy())
+
+
+def test_host_buffer_is_pinned_and_zero(backend):
+    buf = backend.host_buffer(12, "complex64")
+    assert buf.is_pinned() and buf.numel() == 4096 and str(buf.dtype) == "torch.complex64"
+    assert not bool(buf.abs().max() > 0)
+    d = backend.cast(buf, dtype="complex64")
+    assert d.is_cuda and d.numel() == 4096
