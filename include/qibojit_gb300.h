@@ -204,11 +204,13 @@ typedef struct sv_gate_op {
 typedef struct sv_program sv_program;
 
 /* Plans and uploads a program for states of `nqubits` qubits and type `dtype`
- * (SV_C128 or SV_C64).  tile_bits <= 0 picks the default (11 for complex128, 12 for
- * complex64).  The op list is read before the call returns.  The planner writes each
- * uncontrolled one-qubit gate as diag * real 2x2 * diag and carries the diagonals to
- * the next gate on their qubit (they commute with every diagonal gate), folding those
- * of a phase into one table: the same unitary with fewer multiply-adds. */
+ * (SV_C128 or SV_C64).  tile_bits <= 0 picks the default (12: 2^12 amplitudes per
+ * tile).  The op list is read before the call returns.  Each pass's ops are grouped
+ * into register phases by dependency, so a block of qubits runs several layers per
+ * shared-memory exchange.  Complex128 programs (and complex64 programs once
+ * specialised) are also phase-folded: each uncontrolled one-qubit gate becomes
+ * diag * real 2x2 * diag with the diagonals carried to the next gate on their qubit
+ * and folded per phase into one table, the same unitary with fewer multiply-adds. */
 int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op* ops, int nops,
                        int tile_bits, sv_program** out);
 /* Applies the program to `state` (device, 2^nqubits amplitudes) on the context's stream. */
