@@ -96,3 +96,44 @@ def test_large_brickwork_specialised_matches_interpreted(backend, dt):
     tol = 1e-6 if dt == "complex64" else 1e-13
     assert backend.max_abs_diff(a, b, n) < tol
     assert abs(backend.norm2(b, n) - 1) < (1e-5 if dt == "complex64" else 1e-12)
+
+
+def _families(n, kind, seed):
+    from qibojit_gb300 import gates as G
+
+    rng = np.random.default_rng(seed)
+    c = G.Circuit(n)
+    for _ in range(6 * n):
+        q = [int(x) for x in rng.permutation(n)]
+        t = float(rng.uniform(0, 2 * np.pi))
+        if kind == "diagonal":
+            c.add([G.CZ(q[0], q[1]), G.RZ(q[0], t), G.CU1(q[0], q[1], t), G.T(q[0]), G.Z(q[0]),
+                   G.CCZ(q[0], q[1], q[2])][int(rng.integers(6))])
+        elif kind == "permutation":
+            c.add([G.X(q[0]), G.CNOT(q[0], q[1]), G.SWAP(q[0], q[1]), G.TOFFOLI(q[0], q[1], q[2])][int(rng.integers(4))])
+        else:  # real rotations and Hadamards
+            c.add([G.RY(q[0], t), G.H(q[0])][int(rng.integers(2))])
+    return c
+
+
+@pytest.mark.parametrize("kind", ["diagonal", "permutation", "real"])
+@pytest.mark.parametrize("n,tile_bits", [(8, 8), (13, 0)])
+def test_special_gate_families_specialised(backend, kind, n, tile_bits, dtype):
+    """Circuits of only diagonal, only permutation or only real gates (no folding
+    material, sign tables only, runs of real rotations) at the smallest state a fused
+    program takes (n = 8, one tile) and at n = 13."""
+    circ = _families(n, kind, 31)
+    state = random_state(n, 32, dtype)
+    spec = backend.compile(circ, dtype, tile_bits=tile_bits, specialize=True)
+    got = backend.to_numpy(spec.run(backend.cast(state, dtype=dtype, copy=True)))
+    want = backend.to_numpy(backend.execute_circuit(circ, backend.cast(state, dtype=dtype, copy=True), fuse=False))
+    np.testing.assert_allclose(got, want, rtol=0, atol=PARITY_ATOL[dtype] * (10 if dtype == "complex64" else 1))
+
+
+def test_empty_circuit_specialised(backend):
+    from qibojit_gb300 import gates as G
+
+    x = random_state(10, 33, "complex64")
+    prog = backend.compile(G.Circuit(10), "complex64", specialize=True)
+    got = backend.to_numpy(prog.run(backend.cast(x, dtype="complex64", copy=True)))
+    np.testing.assert_array_equal(got, x)
