@@ -16,8 +16,10 @@ result's infidelity and max amplitude error against the complex128 state.
 of one pass (2 x 8 B x 2^30, one read and one write of the state) / its mean duration
 from CUDA events over the timed region; FP32 arithmetic is reported beside it
 (16 flops per amplitude per dense one-qubit gate).  ``e2e`` repeats the metric
-through the public backend API (``execute_circuit``) with the initial state uploaded
-from pinned host memory and the final state read back every step.
+through the public backend API (``execute_circuit_stream``) with every step's initial
+state uploaded from pinned host memory and its final state read back, the copies of
+neighbouring steps overlapped with the passes; ``sequential_value`` is the same through
+``execute_circuit`` one call at a time.
 ``cpu_baseline`` and ``--impl reference`` time the CPU restatement of the reference's
 Numba kernels (per-gate, OpenMP, all host threads) on the first layer of the circuit.
 """
@@ -257,16 +259,25 @@ def run_engine(args):
     host_in = backend.host_buffer(n, dtype)  # pinned, on the GPU's local memory node
     host_in[0] = 1
     host_out = backend.host_buffer(n, dtype)
-    e2e_steps = max(1, min(args.steps, 3))
     for _ in range((backend.specialize_after or 0) + 1):  # plans, caches and specialises the program
         backend.execute_circuit(circ, host_in)
     torch.cuda.synchronize()
+    # one call at a time: upload, passes and read-back in sequence
+    seq_steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(seq_steps):
         s = backend.execute_circuit(circ, host_in)
         host_out.copy_(s)
         del s
     torch.cuda.synchronize()
+    e2e_seq_value = ws * ngates * seq_steps / (time.perf_counter() - t0)
+    # pipelined: execute_circuit_stream overlaps step k+1's upload and step k-1's
+    # read-back with step k's passes (every step still moves the whole state both ways)
+    e2e_steps = max(3, min(2 * args.steps, 8))
+    backend.execute_circuit_stream(circ, [host_in], [host_out])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    backend.execute_circuit_stream(circ, [host_in] * e2e_steps, [host_out] * e2e_steps)
     e2e_value = ws * ngates * e2e_steps / (time.perf_counter() - t0)
     final64 = host_out  # |psi> of the complex64 fused run, on the host
 
@@ -346,7 +357,8 @@ def run_engine(args):
                          "dense_u3_equivalent_frac_of_fp32_probe_peak": fp32_tflops / FP32_PEAK_TFLOPS},
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "steps": e2e_steps},
+                    "steps": e2e_steps, "api": "execute_circuit_stream (pinned host states, copies overlapped)",
+                    "sequential_value": e2e_seq_value, "sequential_steps": seq_steps},
             "gpu_launches": args.steps * (st["passes"] + 1),
             "clocks": clocks.summary(),
             "variants": variants,

@@ -489,21 +489,82 @@ class GB300Backend(_QiboBackend):
                 state = self.apply_gate(gate, state, n)
             return state
         if fuse and n >= 8 and dtype in ("complex128", "complex64") and circuit.queue:
-            key = (id(circuit), len(circuit.queue), n, dtype)
-            prog = self._programs.get(key)
-            if prog is None:
-                prog = self.compile(circuit, dtype)
-                self._programs = {key: prog}
-            elif not prog.specialized and self.specialize_after is not None and prog.runs >= self.specialize_after:
-                # a program run repeatedly: re-plan on the larger tile and compile its passes
-                runs = prog.runs
-                prog = self.compile(circuit, dtype, specialize=True)
-                prog.runs = runs
-                self._programs = {key: prog}
-            return prog.run(state)
+            return self._cached_program(circuit, dtype).run(state)
         for gate in circuit.queue:
             state = self.apply_gate(gate, state, n)
         return state
+
+    def _cached_program(self, circuit, dtype: str, upcoming_runs: int = 1):
+        """The program cache of execute_circuit (one entry): a program that has run
+        ``specialize_after`` times (counting the runs about to be made) is re-planned on
+        the larger tile and its passes specialised."""
+        key = (id(circuit), len(circuit.queue), circuit.nqubits, dtype)
+        prog = self._programs.get(key)
+        if prog is None:
+            prog = self.compile(circuit, dtype)
+            self._programs = {key: prog}
+        if (not prog.specialized and self.specialize_after is not None
+                and prog.runs + upcoming_runs - 1 >= self.specialize_after):
+            runs = prog.runs
+            prog = self.compile(circuit, dtype, specialize=True)
+            prog.runs = runs
+            self._programs = {key: prog}
+        return prog
+
+    def execute_circuit_stream(self, circuit, host_inputs, host_outputs):
+        """Runs ``circuit`` on each pinned host state of ``host_inputs`` and writes each
+        final state into the matching pinned tensor of ``host_outputs``.
+
+        States move through two device buffers on three CUDA streams: the upload of
+        state k+1 and the read-back of state k-1 run while state k's passes do, so both
+        directions of the host link and the GPU work at once.  Inputs may repeat (the
+        same tensor for every k) and so may outputs (written in order, the last state
+        wins); an output must not be a later step's input.  Returns when every state is
+        back on the host."""
+        torch = _torch()
+        k_total = len(host_inputs)
+        if len(host_outputs) != k_total:
+            raise ValueError("need one output per input state")
+        if k_total == 0:
+            return host_outputs
+        n = circuit.nqubits
+        dtype = _dtype_name(host_inputs[0].dtype)
+        if n < 8 or dtype not in ("complex128", "complex64") or not circuit.queue:
+            for x, y in zip(host_inputs, host_outputs):
+                y.copy_(self.execute_circuit(circuit, x))
+            return host_outputs
+        for t in list(host_inputs) + list(host_outputs):
+            if t.is_cuda or t.numel() != (1 << n) or _dtype_name(t.dtype) != dtype:
+                raise ValueError(f"host states must hold 2^{n} {dtype} amplitudes")
+        prog = self._cached_program(circuit, dtype, k_total)
+        tdt = _torch_dtype(dtype)
+        dev = [torch.empty(1 << n, dtype=tdt, device=self._tdevice) for _ in range(min(2, k_total))]
+        up, comp, down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        freed = [None] * len(dev)
+        self.ctx.set_stream(comp.cuda_stream)
+        try:
+            for k in range(k_total):
+                b = k % len(dev)
+                with torch.cuda.stream(up):
+                    if freed[b] is not None:
+                        up.wait_event(freed[b])
+                    dev[b].copy_(host_inputs[k], non_blocking=True)
+                    loaded = torch.cuda.Event()
+                    loaded.record(up)
+                comp.wait_event(loaded)
+                prog.run(dev[b])
+                computed = torch.cuda.Event()
+                computed.record(comp)
+                with torch.cuda.stream(down):
+                    down.wait_event(computed)
+                    host_outputs[k].copy_(dev[b], non_blocking=True)
+                    freed[b] = torch.cuda.Event()
+                    freed[b].record(down)
+        finally:
+            for st in (up, comp, down):
+                st.synchronize()
+            self.ctx.set_stream(0)
+        return host_outputs
 
     # --------------------------------------------------------- FP64 reductions
     def inner_product(self, a, b, nqubits: int) -> complex:
