@@ -142,6 +142,23 @@ int sv_collapse_state_noalloc(void* stream, void* state, int dtype, int nqubits,
 int sv_probabilities(sv_context* ctx, const void* state, int dtype, int nqubits,
                      const int32_t* qubits, int nq, void* out, int out_dtype);
 
+/* ------------------------------------------------------- density matrices */
+/* Marginal probabilities of an n-qubit density matrix `rho` (row-major
+ * 2^n x 2^n, 2n <= 40): out[o] = sum of Re rho_ii over the basis states i whose
+ * measured bits read o, qubits ordered as given (qibo's density-matrix
+ * calculate_probabilities, the branch CupyBackend.calculate_probabilities
+ * forwards at gpu.py:751-768).  Same output rules as sv_probabilities. */
+int sv_density_probabilities(sv_context* ctx, const void* rho, int dtype, int nqubits,
+                             const int32_t* qubits, int nq, void* out, int out_dtype);
+
+/* y <- a x + b y over n elements of `dtype` (complex coefficients for complex
+ * arrays; a_im = b_im = 0 for real ones).  With b = 0 y is only written.  x and
+ * y may be the same array.  The accumulation of NumbaBackend
+ * _apply_channel_density_matrix (cpu.py:400-415):
+ * new = (1 - sum c) rho + sum_k c_k U_k rho U_k^dagger. */
+int sv_axpby(sv_context* ctx, int dtype, int64_t n, const void* x, double a_re,
+             double a_im, void* y, double b_re, double b_im);
+
 /* ------------------------------------------------------------- sampling */
 /* Metropolis sampling of `nshots` outcomes from `probs` (2^nbits entries,
  * SV_F64 or SV_F32), `nchains` independent chains, accumulated into the int64

@@ -319,3 +319,80 @@ class OracleBackend:
 
     def zero_state(self, nqubits, dtype="complex128"):
         return initial_state_vector(np.empty(1 << nqubits, dtype=dtype))
+
+
+# --- density matrices ---------------------------------------------------------------
+def apply_gate_density_matrix(backend: OracleBackend, rho: np.ndarray, nqubits: int, targets, controls,
+                              kernel: str, gate) -> np.ndarray:
+    """rho -> U rho U^dagger on the 2n-qubit vector of the row-major rho, as
+    ``_apply_gate_density_matrix`` / ``_apply_ygate_density_matrix`` (cpu.py:452-517):
+    the gate's kernel with ``qubits + n`` on the row qubits, then with conj(gate) and
+    ``qubits`` on the column qubits ``t + n``.  Y and CY run ``apply_y`` on the rows and
+    ``apply_gate`` with conj(Y) on the columns.  ``kernel`` is the one- or two-target
+    kernel name, or "multi" for ``_multi_qubit_base``."""
+    flat = rho.reshape(-1)
+    qubits = backend.qubits_tensor(nqubits, targets, controls)
+    qubits_dm = qubits + nqubits
+    targets_dm = [t + nqubits for t in targets]
+    n2 = 2 * nqubits
+    conj = np.conj(gate) if isinstance(gate, np.ndarray) or np.iscomplexobj(gate) else gate
+    if kernel == "apply_y":
+        backend._one_qubit_base(flat, n2, targets[0], "apply_y", gate, qubits_dm)
+        backend._one_qubit_base(flat, n2, targets_dm[0], "apply_gate", np.conj(gate), qubits)
+    elif kernel == "multi":
+        backend._multi_qubit_base(flat, n2, list(targets), gate, qubits_dm)
+        backend._multi_qubit_base(flat, n2, targets_dm, conj, qubits)
+    elif len(targets) == 1:
+        backend._one_qubit_base(flat, n2, targets[0], kernel, gate, qubits_dm)
+        backend._one_qubit_base(flat, n2, targets_dm[0], kernel, conj, qubits)
+    else:
+        backend._two_qubit_base(flat, n2, targets[0], targets[1], kernel, gate, qubits_dm)
+        backend._two_qubit_base(flat, n2, targets_dm[0], targets_dm[1], kernel, conj, qubits)
+    return rho
+
+
+def apply_channel_density_matrix(rho: np.ndarray, coefficients: Sequence[float], branches) -> np.ndarray:
+    """``_apply_channel_density_matrix`` (cpu.py:400-415): (1 - sum c) rho + sum_k c_k
+    U_k rho U_k^dagger.  ``branches[k]`` applies U_k to a density matrix in place; every
+    branch starts from a copy of rho (the reference undoes unitary branches with the
+    inverse gate instead, which agrees to rounding)."""
+    new = (1 - float(sum(coefficients))) * rho
+    for c, apply in zip(coefficients, branches):
+        work = rho.copy()
+        apply(work)
+        new += float(c) * work
+    return new
+
+
+def density_probabilities(rho: np.ndarray, qubits: Sequence[int], nqubits: int) -> np.ndarray:
+    """Re diag(rho) marginalised on ``qubits``, ordered as given (qubits[0] the most
+    significant output bit), summed in FP64: the density-matrix branch of qibo's
+    ``calculate_probabilities`` (a third-party method, restated from its definition)."""
+    d = np.real(np.diagonal(np.asarray(rho).reshape(1 << nqubits, 1 << nqubits))).astype(np.float64)
+    d = d.reshape((2,) * nqubits)
+    rest = tuple(q for q in range(nqubits) if q not in qubits)
+    marg = d.sum(axis=rest) if rest else d
+    kept = [q for q in range(nqubits) if q in qubits]  # axes left, ascending
+    marg = np.transpose(marg, [kept.index(q) for q in qubits])
+    return np.ascontiguousarray(marg).reshape(-1)
+
+
+def collapse_density_matrix(rho: np.ndarray, qubits: Sequence[int], shot: int, nqubits: int,
+                            normalize: bool = True) -> np.ndarray:
+    """P rho P (/ tr(P rho P)) in place, P projecting ``qubits`` onto the bits of ``shot``
+    (qubits[0] its most significant bit): qibo's density-matrix collapse, restated."""
+    dim = 1 << nqubits
+    m = np.asarray(rho).reshape(dim, dim)
+    idx = np.arange(dim)
+    keep = np.ones(dim, dtype=bool)
+    k = len(qubits)
+    for j, q in enumerate(qubits):
+        bit = (shot >> (k - 1 - j)) & 1
+        keep &= ((idx >> (nqubits - 1 - q)) & 1) == bit
+    p = float(np.sum(np.real(np.diagonal(m))[keep], dtype=np.float64))
+    m[~keep, :] = 0
+    m[:, ~keep] = 0
+    if normalize:
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m *= np.float64(1.0) / np.float64(p)
+    return rho

@@ -26,7 +26,8 @@ TWO_KINDS = {"apply_two_qubit_gate": 0, "apply_swap": 1, "apply_fsim": 2}
 EXPORTS = (
     "sv_version", "sv_last_error", "sv_device_count", "sv_context_create", "sv_context_destroy",
     "sv_context_set_stream", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
-    "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_measure_frequencies",
+    "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_density_probabilities", "sv_axpby",
+    "sv_measure_frequencies",
     "sv_collapse_state_noalloc", "sv_sample_cdf", "sv_program_create", "sv_program_run", "sv_program_stats", "sv_program_specialize",
     "sv_program_destroy", "sv_inner_product", "sv_max_abs_diff", "sv_expectation_z",
     "sv_batch_create", "sv_batch_run", "sv_batch_tfim_energy", "sv_batch_state", "sv_batch_stats",
@@ -61,6 +62,9 @@ _SIGNATURES = {
     "sv_apply_multi_qubit": ([_vp, _vp, _int, _int, _vp, _vp, _int, _vp, _int], _int),
     "sv_collapse_state": ([_vp, _vp, _int, _int, _vp, _int, _i64, _int], _int),
     "sv_probabilities": ([_vp, _vp, _int, _int, _vp, _int, _vp, _int], _int),
+    "sv_density_probabilities": ([_vp, _vp, _int, _int, _vp, _int, _vp, _int], _int),
+    "sv_axpby": ([_vp, _int, ctypes.c_int64, _vp, ctypes.c_double, ctypes.c_double, _vp, ctypes.c_double,
+                  ctypes.c_double], _int),
     "sv_measure_frequencies": ([_vp, _vp, _vp, _int, _int, _i64, ctypes.c_uint32, _int], _int),
     "sv_collapse_state_noalloc": ([_vp, _vp, _int, _int, _vp, _int, _i64, _int], _int),
     "sv_program_create": ([_vp, _int, _int, _vp, _int, _int, ctypes.POINTER(_vp)], _int),

@@ -84,6 +84,12 @@ def _torch_dtype(name: str):
     return _TORCH_DTYPES[name]
 
 
+def _is_channel(gate) -> bool:
+    """A qibo noise channel as NumbaBackend.apply_channel consumes it (cpu.py:400-415):
+    coefficients with one gate each."""
+    return hasattr(gate, "coefficients") and hasattr(gate, "gates")
+
+
 def _dtype_name(x) -> str:
     s = str(x)
     return s.replace("torch.", "").replace("numpy.", "").replace("<class '", "").replace("'>", "")
@@ -224,11 +230,55 @@ class GB300Backend(_QiboBackend):
             return self._apply_gate_density_matrix(gate, state, nqubits, inverse)
         return self._apply_gate(gate, state, nqubits)
 
+    def apply_channel(self, channel, state, nqubits: int):
+        """A noise channel sum_k c_k U_k (cpu.py:359-367).  On a density matrix every
+        branch is applied (cpu.py:400-415); on a state vector one branch is drawn from
+        the coefficients (the rest of the probability keeps the state) with NumPy's
+        global stream."""
+        if len(tuple(state.shape)) == 2:
+            return self._apply_channel_density_matrix(channel, state, nqubits)
+        coeffs = [float(c) for c in channel.coefficients]
+        probs = np.array(coeffs + [1.0 - sum(coeffs)], dtype=np.float64)
+        index = int(np.random.choice(len(probs), p=probs))
+        if index < len(channel.gates):
+            state = self.apply_gate(channel.gates[index], state, nqubits)
+        return state
+
+    def _apply_channel_density_matrix(self, channel, state, nqubits: int):
+        """new = (1 - sum c) rho + sum_k c_k U_k rho U_k^dagger (cpu.py:400-415), each
+        branch on a copy of rho and accumulated by ``sv_axpby``.  The reference restores
+        rho between branches by applying the inverse gate (unitary channels) or from a
+        copy; here every branch starts from a copy, and the input is left unchanged."""
+        torch = _torch()
+        dt = self._check_state(state, 2 * int(nqubits))
+        numel = state.numel()
+        coeffs = [float(c) for c in channel.coefficients]
+        total = float(getattr(channel, "coefficient_sum", sum(coeffs)))
+        new = torch.empty_like(state)
+        _lib.check(self.lib.sv_axpby(self.ctx.handle, dt, numel, state.data_ptr(), 1.0 - total, 0.0, new.data_ptr(),
+                                     0.0, 0.0), "apply_channel")
+        work = torch.empty_like(state)
+        for coeff, gate in zip(coeffs, channel.gates):
+            work.copy_(state)
+            work = self._apply_gate_density_matrix(gate, work, nqubits)
+            _lib.check(self.lib.sv_axpby(self.ctx.handle, dt, numel, work.data_ptr(), coeff, 0.0, new.data_ptr(),
+                                         1.0, 0.0), "apply_channel")
+        return new
+
     def _apply_gate_density_matrix(self, gate, state, nqubits: int, inverse: bool = False):
         """rho -> U rho U^dagger as two calls on the 2n-qubit vector (cpu.py:452-498): U
         on the row qubits (bits shifted up by n), conj(U) on the column qubits."""
         name = type(gate).__name__
         dtype = _dtype_name(state.dtype)
+        if getattr(gate, "name", "") == "fanout":  # one CNOT per target, as on state vectors
+            shape, n2, x = state.shape, 2 * nqubits, self.custom_matrices.X
+            flat = state.reshape(-1)
+            control = gate.control_qubits[0]
+            for t in gate.target_qubits:
+                q = np.array(sorted([nqubits - control - 1, nqubits - t - 1]), dtype=np.int32)
+                flat = self._one_qubit_base(flat, n2, t, "apply_x", x, q + nqubits)
+                flat = self._one_qubit_base(flat, n2, t + nqubits, "apply_x", x, q)
+            return flat.reshape(shape)
         if inverse:
             u = np.linalg.inv(np.asarray(gate.matrix(self)))
             matrix = u if len(gate.control_qubits) == 0 else None
@@ -348,34 +398,61 @@ class GB300Backend(_QiboBackend):
     # ------------------------------------------------------------------ collapse
     def collapse_state(self, state, qubits: Sequence[int], shot, nqubits: int, normalize: bool = True,
                        density_matrix: bool = False):
-        if density_matrix:
-            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
-        dt = self._check_state(state, nqubits)
         if hasattr(shot, "shape"):
             shot = int(np.asarray(self.to_numpy(shot)).ravel()[0])
         elif hasattr(shot, "__len__"):
             shot = int(shot[0])
+        if density_matrix or len(tuple(state.shape)) == 2:
+            return self._collapse_density_matrix(state, qubits, shot, nqubits, normalize)
+        dt = self._check_state(state, nqubits)
         q, nq = _lib.int32_array(list(qubits))
         rc = self.lib.sv_collapse_state(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, int(shot),
                                         int(bool(normalize)))
         _lib.check(rc, "collapse_state")
         return state
 
+    def _collapse_density_matrix(self, rho, qubits: Sequence[int], shot: int, nqubits: int, normalize: bool):
+        """rho -> P rho P (/ tr(P rho P)), P the projector of ``qubits`` onto the bits of
+        ``shot`` (qubits[0] its most significant bit), in place.  On the 2n-qubit vector of
+        rho this is the state-vector collapse of the row qubits and the column qubits
+        (q + n) onto the shot twice over; the trace is the outcome's probability, taken
+        from rho's diagonal before the projection."""
+        n = int(nqubits)
+        dt = self._check_state(rho, 2 * n)
+        k = len(qubits)
+        if not 0 <= shot < (1 << k):
+            raise ValueError(f"shot {shot} is not an outcome of {k} qubits")
+        if normalize:
+            p = float(self.calculate_probabilities(rho, qubits, n, density_matrix=True,
+                                                   out_dtype="float64")[shot].item())
+        q, nq = _lib.int32_array(list(qubits) + [int(x) + n for x in qubits])
+        rc = self.lib.sv_collapse_state(self.ctx.handle, rho.data_ptr(), dt, 2 * n, q, nq, (shot << k) | shot, 0)
+        _lib.check(rc, "collapse_state")
+        if normalize:
+            with np.errstate(divide="ignore"):
+                scale = float(np.float64(1.0) / np.float64(p))
+            _lib.check(self.lib.sv_axpby(self.ctx.handle, dt, rho.numel(), rho.data_ptr(), scale, 0.0,
+                                         rho.data_ptr(), 0.0, 0.0), "collapse_state")
+        return rho
+
     # -------------------------------------------------------------- probabilities
     def calculate_probabilities(self, state, qubits: Sequence[int], nqubits: int, density_matrix: bool = False,
                                 out_dtype: Optional[str] = None):
         """|psi|^2 marginalised on ``qubits``; float64 for complex128 states and float32
         for complex64 states (the state's real type, as qibo returns), summed in FP64."""
-        if density_matrix:
-            raise NotImplementedError("density matrices are outside the gb300 engine's scope")
-        dt = self._check_state(state, nqubits)
+        if density_matrix:  # the real diagonal of rho, marginalised the same way
+            dt = self._check_state(state, 2 * int(nqubits))
+            entry = self.lib.sv_density_probabilities
+        else:
+            dt = self._check_state(state, nqubits)
+            entry = self.lib.sv_probabilities
         if out_dtype is None:
             out_dtype = "float64" if dt in (_lib.SV_C128, _lib.SV_F64) else "float32"
         torch = _torch()
         out = torch.empty(1 << len(qubits), dtype=_torch_dtype(out_dtype), device=self._tdevice)
         q, nq = _lib.int32_array(list(qubits))
-        rc = self.lib.sv_probabilities(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, out.data_ptr(),
-                                       _lib.DTYPE_CODES[out_dtype])
+        rc = entry(self.ctx.handle, state.data_ptr(), dt, int(nqubits), q, nq, out.data_ptr(),
+                   _lib.DTYPE_CODES[out_dtype])
         _lib.check(rc, "calculate_probabilities")
         return out
 
@@ -452,15 +529,20 @@ class GB300Backend(_QiboBackend):
         return Counter(dict(zip(idx.cpu().tolist(), freqs[idx].cpu().tolist())))
 
     # ---------------------------------------------------------------- execution
-    def compile(self, circuit, dtype: Optional[str] = None, tile_bits: int = 0, specialize: bool = False):
+    def compile(self, circuit, dtype: Optional[str] = None, tile_bits: int = 0, specialize: bool = False,
+                density_matrix: bool = False):
         """Plans ``circuit`` into fused HBM passes (see ``qibojit_gb300.fusion``); with
-        ``specialize`` also compiles pass kernels for its structure (seconds, once)."""
-        from .fusion import FusedProgram
+        ``specialize`` also compiles pass kernels for its structure (seconds, once).  With
+        ``density_matrix`` the program acts on the flattened 2^n x 2^n density matrix, a
+        2n-qubit vector (each gate as U on the row qubits and conj(U) on the columns)."""
+        from .fusion import FusedProgram, lower_density
 
         dtype = dtype or self.dtype
+        nbits = 2 * circuit.nqubits if density_matrix else circuit.nqubits
         if specialize and not tile_bits:
-            tile_bits = self._specialized_tile_bits(dtype, circuit.nqubits)
-        prog = FusedProgram(self.ctx, circuit.queue, circuit.nqubits, dtype, tile_bits)
+            tile_bits = self._specialized_tile_bits(dtype, nbits)
+        ops = lower_density(circuit.queue, circuit.nqubits) if density_matrix else None
+        prog = FusedProgram(self.ctx, circuit.queue, nbits, dtype, tile_bits, ops=ops)
         return prog.specialize() if specialize else prog
 
     @staticmethod
@@ -484,29 +566,34 @@ class GB300Backend(_QiboBackend):
                               copy=True)
         dtype = _dtype_name(state.dtype)
         fuse = self.fusion if fuse is None else fuse
-        if state.dim() == 2:  # density matrix: gate by gate, U on rows and conj(U) on columns
-            for gate in circuit.queue:
-                state = self.apply_gate(gate, state, n)
+        density = state.dim() == 2
+        nbits = 2 * n if density else n
+        channels = any(_is_channel(g) for g in circuit.queue)
+        if fuse and nbits >= 8 and dtype in ("complex128", "complex64") and circuit.queue and not channels:
+            # a density matrix runs as the 2n-qubit vector of rho: U on rows, conj(U) on columns
+            flat = state.reshape(-1)
+            self._cached_program(circuit, dtype, density_matrix=density).run(flat)
             return state
-        if fuse and n >= 8 and dtype in ("complex128", "complex64") and circuit.queue:
-            return self._cached_program(circuit, dtype).run(state)
         for gate in circuit.queue:
-            state = self.apply_gate(gate, state, n)
+            if _is_channel(gate):
+                state = self.apply_channel(gate, state, n)
+            else:
+                state = self.apply_gate(gate, state, n)
         return state
 
-    def _cached_program(self, circuit, dtype: str, upcoming_runs: int = 1):
+    def _cached_program(self, circuit, dtype: str, upcoming_runs: int = 1, density_matrix: bool = False):
         """The program cache of execute_circuit (one entry): a program that has run
         ``specialize_after`` times (counting the runs about to be made) is re-planned on
         the larger tile and its passes specialised."""
-        key = (id(circuit), len(circuit.queue), circuit.nqubits, dtype)
+        key = (id(circuit), len(circuit.queue), circuit.nqubits, dtype, bool(density_matrix))
         prog = self._programs.get(key)
         if prog is None:
-            prog = self.compile(circuit, dtype)
+            prog = self.compile(circuit, dtype, density_matrix=density_matrix)
             self._programs = {key: prog}
         if (not prog.specialized and self.specialize_after is not None
                 and prog.runs + upcoming_runs - 1 >= self.specialize_after):
             runs = prog.runs
-            prog = self.compile(circuit, dtype, specialize=True)
+            prog = self.compile(circuit, dtype, specialize=True, density_matrix=density_matrix)
             prog.runs = runs
             self._programs = {key: prog}
         return prog

@@ -396,10 +396,12 @@ static void merge_signs(FOp* ops, int begin, int* end) {
 
 // Folds runs of register-only diagonals of a phase (one-bit diagonals on register
 // slots, sign diagonals without thread or tile bits) into one FOP_DIAGR table of 16
-// complex factors, one multiply per amplitude for the whole run.  One-bit register
-// diagonals are first moved ahead of the mixing ops on other slots just before them
-// (they commute), which gathers the diagonals that a layer of one-qubit gates leaves
-// in front of it.  Table entries are products of the ops' FP64 entries.
+// complex factors, one multiply per amplitude for the whole run.  These foldable
+// diagonals are first regrouped: each may sit anywhere between the mixing ops on its
+// own slots before and after it (it commutes with the rest, diagonals included), and
+// the fewest common positions that hold every one of them are chosen greedily (interval
+// stabbing: each position is the right end of the earliest-ending interval not yet
+// held).  Table entries are products of the ops' FP64 entries.
 template <typename T>
 static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, int begin, int* end, int* ncoef,
                                     int* slack, std::vector<int32_t>* src) {
@@ -420,21 +422,72 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
       if (f.tb[i] >= 0 || f.ob[i] >= 0) return false;
     return true;
   };
-  for (int r = begin + 1; r < *end; r++) {
-    const int u = diag_slot(pp->ops[r]);
-    if (u < 0) continue;
-    const FOp f = pp->ops[r];
-    int q = r;
-    while (q > begin) {
-      const FOp& g = pp->ops[q - 1];
-      const bool two = g.type == FOP_DENSE2 || g.type == FOP_SWAP2;
-      const bool mixing = two || g.type == FOP_DENSE1 || g.type == FOP_DENSE1R || g.type == FOP_DENSE1P ||
-                          g.type == FOP_X1;
-      if (!mixing || g.u0 == u || (two && g.u1 == u)) break;  // controls on slot u commute with it
-      pp->ops[q] = g;
-      q--;
+  // register slots a foldable diagonal depends on
+  auto fold_slots = [&](const FOp& f) -> unsigned {
+    const int u = diag_slot(f);
+    if (u >= 0) return 1u << u;
+    unsigned m = 0;
+    for (int v = 0; v < kRB; v++)
+      for (int j = 0; j < 16; j++)
+        if (((f.neg[0] >> j) & 1) != ((f.neg[0] >> (j ^ (1 << v))) & 1)) m |= 1u << v;
+    return m;
+  };
+  // register slots whose diagonals a fixed op does not commute with (all 4: unknown kind)
+  auto mixing_slots = [](const FOp& g) -> unsigned {
+    switch (g.type) {
+      case FOP_DENSE1: case FOP_DENSE1R: case FOP_DENSE1P: case FOP_X1: return 1u << g.u0;
+      case FOP_DENSE2: case FOP_SWAP2: return (1u << g.u0) | (1u << g.u1);
+      case FOP_D1RUN: case FOP_D1RUNR: {
+        unsigned m = 0;
+        for (int k = 0; k < g.nrun; k++) m |= 1u << g.ru[k];
+        return m;
+      }
+      case FOP_DIAG: case FOP_SIGN: case FOP_DIAGR: return 0u;
+      default: return 0xfu;
     }
-    pp->ops[q] = f;
+  };
+  {
+    std::vector<FOp> fixed, fold;
+    std::vector<int> gap, lo, hi;  // per foldable: fixed ops before it, interval of gaps
+    for (int r = begin; r < *end; r++) {
+      const FOp& f = pp->ops[r];
+      if (diag_slot(f) >= 0 || reg_sign(f)) {
+        fold.push_back(f);
+        gap.push_back((int)fixed.size());
+      } else {
+        fixed.push_back(f);
+      }
+    }
+    const int nf = (int)fold.size(), m = (int)fixed.size();
+    if (nf > 1) {
+      lo.resize(nf);
+      hi.resize(nf);
+      for (int i = 0; i < nf; i++) {
+        const unsigned sl = fold_slots(fold[i]);
+        int a = gap[i];
+        while (a > 0 && !(mixing_slots(fixed[a - 1]) & sl)) a--;
+        int b = gap[i];
+        while (b < m && !(mixing_slots(fixed[b]) & sl)) b++;
+        lo[i] = a;
+        hi[i] = b;
+      }
+      std::vector<int> order(nf), at(nf, -1);
+      for (int i = 0; i < nf; i++) order[i] = i;
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hi[x] < hi[y]; });
+      for (int k = 0; k < nf; k++) {
+        const int i = order[k];
+        if (at[i] >= 0) continue;
+        const int pnt = hi[i];
+        for (int j = 0; j < nf; j++)
+          if (at[j] < 0 && lo[j] <= pnt && pnt <= hi[j]) at[j] = pnt;
+      }
+      int w = begin;
+      for (int g = 0; g <= m; g++) {
+        for (int i = 0; i < nf; i++)
+          if (at[i] == g) pp->ops[w++] = fold[i];
+        if (g < m) pp->ops[w++] = fixed[g];
+      }
+    }
   }
   int w = begin;
   for (int r = begin; r < *end;) {
@@ -547,11 +600,9 @@ static void pack_phases(const sv_program* prog, const std::vector<int>& sched, c
     for (int i = 0; i < m; i++) {
       if (done[i]) continue;
       if (diag[i]) {
-        // a one-qubit diagonal waits for a phase with its qubit in the registers
-        if (one_diag[i]) {
-          const int lb = local_of[prog->ops[sched[i]].tpos[0]];
-          if (lb < 0 || std::find(bits.begin(), bits.end(), lb) == bits.end()) continue;
-        }
+        // a one-qubit diagonal goes with the first dense op on its qubit (below), in the
+        // phase that op runs in, or to the last phase when no later op needs it
+        if (one_diag[i]) continue;
         if (ready(i)) place(i);
         continue;
       }
@@ -914,33 +965,61 @@ static int build_program(sv_program* prog) {
       int nops = 0, ncoef = 0;
       bool full = false;
       std::vector<int> sched, next;
-      for (int oi : rem) {
-        const HostOp& h = prog->ops[oi];
+      // would op h join now, with `extra_ops` / `extra_coef` taken by ops joining before it
+      auto fits = [&](const HostOp& h, int extra_ops, int extra_coef, bool* fills) {
         uint64_t tbits = 0, bits = 0;
         for (int i = 0; i < h.nt; i++) tbits |= 1ull << h.tpos[i];
         bits = tbits;
         for (int i = 0; i < h.nc; i++) bits |= 1ull << h.cpos[i];
-        const int cc = coef_cost(h);
-        if (full || (bits & blocked) || nops + 1 > max_ops || ncoef + cc > coef_cap) {
-          if (nops + 1 > max_ops || ncoef + cc > coef_cap) full = true;
-          blocked |= bits;
-          next.push_back(oi);
-          continue;
-        }
-        if (dense_like(h)) {
-          const uint64_t need = tbits & ~S;
-          const int nneed = __builtin_popcountll(need);
-          if (ssize + nneed > kt) {
-            blocked |= bits;
-            next.push_back(oi);
-            continue;
-          }
-          S |= need;
-          ssize += nneed;
-        }
+        const bool over = nops + extra_ops + 1 > max_ops || ncoef + extra_coef + coef_cost(h) > coef_cap;
+        *fills = over;
+        if (full || (bits & blocked) || over) return false;
+        return !dense_like(h) || ssize + __builtin_popcountll(tbits & ~S) <= kt;
+      };
+      auto take = [&](int oi) {
+        const HostOp& h = prog->ops[oi];
+        if (dense_like(h))
+          for (int i = 0; i < h.nt; i++)
+            if (!((S >> h.tpos[i]) & 1)) {
+              S |= 1ull << h.tpos[i];
+              ssize++;
+            }
         sched.push_back(oi);
         nops++;
-        ncoef += cc;
+        ncoef += coef_cost(h);
+      };
+      auto leave = [&](int oi, bool fills) {
+        const HostOp& h = prog->ops[oi];
+        if (fills) full = true;
+        for (int i = 0; i < h.nt; i++) blocked |= 1ull << h.tpos[i];
+        for (int i = 0; i < h.nc; i++) blocked |= 1ull << h.cpos[i];
+        next.push_back(oi);
+      };
+      for (size_t k = 0; k < rem.size(); k++) {
+        const int oi = rem[k];
+        const HostOp& h = prog->ops[oi];
+        bool fills = false;
+        // a one-bit diagonal directly before a dense op on the same bit (the phases that
+        // fold_phases carries to the next dense op) goes with that op: left behind alone,
+        // it would cost a full complex multiply here instead of joining the next pass's
+        // register-diagonal table
+        if (h.kind == SV_OP_DIAG && h.nt == 1 && h.nc == 0 && k + 1 < rem.size()) {
+          const HostOp& nx = prog->ops[rem[k + 1]];
+          if (dense_like(nx) && nx.nt == 1 && nx.tpos[0] == h.tpos[0]) {
+            bool fd = false, fn = false;
+            if (fits(h, 0, 0, &fd) && fits(nx, 1, coef_cost(h), &fn)) {
+              take(oi);
+              take(rem[k + 1]);
+            } else {
+              leave(oi, fd || fn);
+              leave(rem[k + 1], false);
+            }
+            k++;
+            continue;
+          }
+        }
+        if (fits(h, 0, 0, &fills)) take(oi);
+        else leave(oi, fills);
       }
       for (int b = 0; b < n && ssize < kt; b++)
         if (!((S >> b) & 1)) {

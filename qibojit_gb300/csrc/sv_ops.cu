@@ -162,43 +162,57 @@ __device__ __forceinline__ int64_t prob_index(int64_t o, int64_t u, const ProbMa
   return i;
 }
 
-template <typename T, typename O>
-__global__ void __launch_bounds__(kOpsBlock) k_probs_full(const T* __restrict__ s, int64_t n,
+// Probability carried by basis index i: |s_i|^2 for a state vector; for a density
+// matrix (DM) the real part of its diagonal element rho_ii, at i * (2^n + 1) in the
+// row-major 2^n x 2^n array (dstride = 2^n + 1).
+template <typename T, bool DM>
+__device__ __forceinline__ double prob_at(const T* __restrict__ s, int64_t i, int64_t dstride) {
+  if constexpr (DM) {
+    const T a = ldg_ro(s + i * dstride);
+    if constexpr (is_complex<T>::value) return (double)a.re;
+    else return (double)a;
+  } else {
+    return tnorm2(ldg_stream(s + i));
+  }
+}
+
+template <typename T, typename O, bool DM>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_full(const T* __restrict__ s, int64_t n, int64_t dstride,
                                                           O* __restrict__ out) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    __stcs(out + i, (O)tnorm2(ldg_stream(s + i)));
+    __stcs(out + i, (O)prob_at<T, DM>(s, i, dstride));
 }
 
-// all qubits measured in a permuted order: out[perm(i)] = |a_i|^2
-template <typename T, typename O>
-__global__ void __launch_bounds__(kOpsBlock) k_probs_perm(const T* __restrict__ s, int64_t n,
+// all qubits measured in a permuted order: out[perm(i)] = p_i
+template <typename T, typename O, bool DM>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_perm(const T* __restrict__ s, int64_t n, int64_t dstride,
                                                           const __grid_constant__ ProbMap p,
                                                           O* __restrict__ out) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     int64_t o = 0;
     for (int j = 0; j < p.nq; j++) o |= ((i >> p.mpos[j]) & 1) << (p.nq - 1 - j);
-    out[o] = (O)tnorm2(ldg_stream(s + i));
+    out[o] = (O)prob_at<T, DM>(s, i, dstride);
   }
 }
 
 // few amplitudes per bin: one thread per bin, sequential sum
-template <typename T, typename O>
-__global__ void __launch_bounds__(kOpsBlock) k_probs_thread_bins(const T* __restrict__ s,
+template <typename T, typename O, bool DM>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_thread_bins(const T* __restrict__ s, int64_t dstride,
                                                                  int64_t nbins, int64_t per_bin,
                                                                  const __grid_constant__ ProbMap p,
                                                                  O* __restrict__ out) {
   const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= nbins) return;
   double acc = 0.0;
-  for (int64_t u = 0; u < per_bin; u++) acc += tnorm2(ldg_stream(s + prob_index(o, u, p)));
+  for (int64_t u = 0; u < per_bin; u++) acc += prob_at<T, DM>(s, prob_index(o, u, p), dstride);
   out[o] = (O)acc;
 }
 
 // many amplitudes per bin: block (segment, bin) sums a contiguous range of u
-template <typename T>
-__global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restrict__ s,
+template <typename T, bool DM>
+__global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restrict__ s, int64_t dstride,
                                                               int64_t per_bin, int nseg,
                                                               const __grid_constant__ ProbMap p,
                                                               double* __restrict__ partials) {
@@ -208,7 +222,7 @@ __global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restric
   const int64_t u0 = (int64_t)seg * len;
   double acc = 0.0;
   for (int64_t u = u0 + threadIdx.x; u < u0 + len; u += blockDim.x)
-    acc += tnorm2(ldg_stream(s + prob_index(o, u, p)));
+    acc += prob_at<T, DM>(s, prob_index(o, u, p), dstride);
   const double r = block_sum(acc);
   if (threadIdx.x == 0) partials[o * nseg + seg] = r;
 }
@@ -466,22 +480,24 @@ static int collapse_typed(Context* ctx, void* state, int nqubits, const Measured
   return SV_OK;
 }
 
-template <typename T, typename O>
+template <typename T, typename O, bool DM = false>
 static int probs_typed(Context* ctx, const void* state, int nqubits, const ProbMap& p, void* out) {
   const int64_t n = (int64_t)1 << nqubits;
+  const int64_t dstride = n + 1;
   const T* s = (const T*)state;
   if (p.nq == nqubits) {
     bool identity = true;
     for (int j = 0; j < p.nq; j++) identity &= (p.mpos[j] == nqubits - 1 - j);
-    if (identity) k_probs_full<T, O><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, (O*)out);
-    else k_probs_perm<T, O><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, p, (O*)out);
+    if (identity) k_probs_full<T, O, DM><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, dstride, (O*)out);
+    else k_probs_perm<T, O, DM><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>(s, n, dstride, p, (O*)out);
     SV_LAUNCH_CHECK("probabilities launch");
     return SV_OK;
   }
   const int64_t nbins = (int64_t)1 << p.nq;
   const int64_t per_bin = (int64_t)1 << (nqubits - p.nq);
   if (per_bin <= 64 || nbins > 65535 || nbins >= (int64_t)ctx->num_sms * 4 * kOpsBlock) {
-    k_probs_thread_bins<T, O><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(s, nbins, per_bin, p, (O*)out);
+    k_probs_thread_bins<T, O, DM><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(s, dstride, nbins, per_bin,
+                                                                                              p, (O*)out);
     SV_LAUNCH_CHECK("probabilities launch");
     return SV_OK;
   }
@@ -494,7 +510,7 @@ static int probs_typed(Context* ctx, const void* state, int nqubits, const ProbM
   SV_TRY(ensure_scratch(ctx, (size_t)(nbins * nseg) * sizeof(double)));
   double* partials = (double*)ctx->scratch;
   dim3 grid((unsigned)nseg, (unsigned)nbins);
-  k_probs_segments<T><<<grid, kOpsBlock, 0, ctx->stream>>>(s, per_bin, (int)nseg, p, partials);
+  k_probs_segments<T, DM><<<grid, kOpsBlock, 0, ctx->stream>>>(s, dstride, per_bin, (int)nseg, p, partials);
   SV_LAUNCH_CHECK("probabilities launch");
   k_probs_finish<O><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(partials, nbins, (int)nseg, (O*)out);
   SV_LAUNCH_CHECK("probabilities finish launch");
@@ -706,6 +722,74 @@ static int sample_cdf_typed(Context* ctx, const void* probs, int nbits, const do
 
 using namespace sv;
 
+template <bool DM>
+static int probabilities_impl(sv_context* ctx, const void* state, int dtype, int nqubits, const int32_t* qubits,
+                              int nq, void* out, int out_dtype) {
+  if (!ctx) return set_error(SV_ERR_ARG, "null context");
+  if (DM && (nqubits < 1 || 2 * nqubits > kMaxQubits))
+    return set_error(SV_ERR_ARG, "density matrix of %d qubits out of range [1, %d]", nqubits, kMaxQubits / 2);
+  SV_TRY(check_state(state, dtype, DM ? 2 * nqubits : nqubits));
+  if (!out) return set_error(SV_ERR_ARG, "output pointer is NULL");
+  if (out_dtype != SV_F64 && out_dtype != SV_F32) return set_error(SV_ERR_ARG, "out_dtype must be SV_F64 or SV_F32");
+  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "probabilities need 1..n qubits");
+  ProbMap p;
+  memset(&p, 0, sizeof(p));
+  p.n = nqubits;
+  p.nq = nq;
+  std::vector<int> sorted;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits) return set_error(SV_ERR_ARG, "qubit %d out of range", qubits[j]);
+    p.mpos[j] = nqubits - qubits[j] - 1;
+    sorted.push_back(p.mpos[j]);
+  }
+  std::sort(sorted.begin(), sorted.end());
+  for (int j = 0; j < nq; j++) {
+    if (j > 0 && sorted[j] == sorted[j - 1]) return set_error(SV_ERR_ARG, "duplicate qubit in probabilities");
+    p.sorted[j] = sorted[j];
+  }
+  const bool f64 = out_dtype == SV_F64;
+  switch (dtype) {
+    case SV_C128: return f64 ? probs_typed<c128, double, DM>(ctx, state, nqubits, p, out) : probs_typed<c128, float, DM>(ctx, state, nqubits, p, out);
+    case SV_C64: return f64 ? probs_typed<c64, double, DM>(ctx, state, nqubits, p, out) : probs_typed<c64, float, DM>(ctx, state, nqubits, p, out);
+    case SV_F64: return f64 ? probs_typed<double, double, DM>(ctx, state, nqubits, p, out) : probs_typed<double, float, DM>(ctx, state, nqubits, p, out);
+    default: return f64 ? probs_typed<float, double, DM>(ctx, state, nqubits, p, out) : probs_typed<float, float, DM>(ctx, state, nqubits, p, out);
+  }
+}
+
+// y <- a x + b y (b == 0: y is only written).  x and y may be the same array.
+template <typename T>
+__global__ void __launch_bounds__(kOpsBlock) k_axpby(const T* x, T* y, int64_t n, double are, double aim,
+                                                     double bre, double bim, bool read_y) {
+  using R = typename real_of<T>::type;
+  const R ar = (R)are, ai = (R)aim, br = (R)bre, bi = (R)bim;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const T u = x[i];
+    if constexpr (is_complex<T>::value) {
+      T r{ar * u.re - ai * u.im, ar * u.im + ai * u.re};
+      if (read_y) {
+        const T v = y[i];
+        r.re += br * v.re - bi * v.im;
+        r.im += br * v.im + bi * v.re;
+      }
+      y[i] = r;
+    } else {
+      R r = ar * u;
+      if (read_y) r += br * y[i];
+      y[i] = r;
+    }
+  }
+}
+
+template <typename T>
+static int axpby_typed(Context* ctx, int64_t n, const void* x, double are, double aim, void* y, double bre,
+                       double bim) {
+  const bool read_y = bre != 0.0 || bim != 0.0;
+  k_axpby<T><<<stream_grid(ctx, n), kOpsBlock, 0, ctx->stream>>>((const T*)x, (T*)y, n, are, aim, bre, bim, read_y);
+  SV_LAUNCH_CHECK("axpby launch");
+  return SV_OK;
+}
+
 extern "C" {
 
 int sv_sample_cdf(sv_context* ctx, const void* probs, int prob_dtype, int nbits, const double* uniforms,
@@ -764,32 +848,30 @@ int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits, cons
 
 int sv_probabilities(sv_context* ctx, const void* state, int dtype, int nqubits, const int32_t* qubits,
                      int nq, void* out, int out_dtype) {
+  return probabilities_impl<false>(ctx, state, dtype, nqubits, qubits, nq, out, out_dtype);
+}
+
+int sv_density_probabilities(sv_context* ctx, const void* rho, int dtype, int nqubits, const int32_t* qubits,
+                             int nq, void* out, int out_dtype) {
+  return probabilities_impl<true>(ctx, rho, dtype, nqubits, qubits, nq, out, out_dtype);
+}
+
+int sv_axpby(sv_context* ctx, int dtype, int64_t n, const void* x, double a_re, double a_im, void* y, double b_re,
+             double b_im) {
   if (!ctx) return set_error(SV_ERR_ARG, "null context");
-  SV_TRY(check_state(state, dtype, nqubits));
-  if (!out) return set_error(SV_ERR_ARG, "output pointer is NULL");
-  if (out_dtype != SV_F64 && out_dtype != SV_F32) return set_error(SV_ERR_ARG, "out_dtype must be SV_F64 or SV_F32");
-  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "probabilities need 1..n qubits");
-  ProbMap p;
-  memset(&p, 0, sizeof(p));
-  p.n = nqubits;
-  p.nq = nq;
-  std::vector<int> sorted;
-  for (int j = 0; j < nq; j++) {
-    if (qubits[j] < 0 || qubits[j] >= nqubits) return set_error(SV_ERR_ARG, "qubit %d out of range", qubits[j]);
-    p.mpos[j] = nqubits - qubits[j] - 1;
-    sorted.push_back(p.mpos[j]);
-  }
-  std::sort(sorted.begin(), sorted.end());
-  for (int j = 0; j < nq; j++) {
-    if (j > 0 && sorted[j] == sorted[j - 1]) return set_error(SV_ERR_ARG, "duplicate qubit in probabilities");
-    p.sorted[j] = sorted[j];
-  }
-  const bool f64 = out_dtype == SV_F64;
+  if (!x || !y) return set_error(SV_ERR_ARG, "x and y are required");
+  if (dtype < SV_C128 || dtype > SV_F32) return set_error(SV_ERR_ARG, "unknown dtype %d", dtype);
+  if (n < 0) return set_error(SV_ERR_ARG, "negative length");
+  if (((uintptr_t)x) % dtype_size(dtype) || ((uintptr_t)y) % dtype_size(dtype))
+    return set_error(SV_ERR_ARG, "arrays are not aligned to their element size");
+  const bool real = dtype == SV_F64 || dtype == SV_F32;
+  if (real && (a_im != 0.0 || b_im != 0.0)) return set_error(SV_ERR_ARG, "complex coefficients on a real array");
+  if (n == 0) return SV_OK;
   switch (dtype) {
-    case SV_C128: return f64 ? probs_typed<c128, double>(ctx, state, nqubits, p, out) : probs_typed<c128, float>(ctx, state, nqubits, p, out);
-    case SV_C64: return f64 ? probs_typed<c64, double>(ctx, state, nqubits, p, out) : probs_typed<c64, float>(ctx, state, nqubits, p, out);
-    case SV_F64: return f64 ? probs_typed<double, double>(ctx, state, nqubits, p, out) : probs_typed<double, float>(ctx, state, nqubits, p, out);
-    default: return f64 ? probs_typed<float, double>(ctx, state, nqubits, p, out) : probs_typed<float, float>(ctx, state, nqubits, p, out);
+    case SV_C128: return axpby_typed<c128>(ctx, n, x, a_re, a_im, y, b_re, b_im);
+    case SV_C64: return axpby_typed<c64>(ctx, n, x, a_re, a_im, y, b_re, b_im);
+    case SV_F64: return axpby_typed<double>(ctx, n, x, a_re, a_im, y, b_re, b_im);
+    default: return axpby_typed<float>(ctx, n, x, a_re, a_im, y, b_re, b_im);
   }
 }
 

@@ -14,7 +14,7 @@ for callers that use the per-gate multi-qubit kernel instead.
 from __future__ import annotations
 
 import ctypes
-from typing import Iterable, List
+from typing import Iterable, List, Optional
 
 import numpy as np
 
@@ -65,15 +65,29 @@ def lower(gates: Iterable) -> List[tuple]:
     return out
 
 
-class FusedProgram:
-    """A circuit planned into fused passes for one state size and dtype."""
+def lower_density(gates: Iterable, nqubits: int) -> List[tuple]:
+    """Gates acting on an n-qubit density matrix rho -> ops on the 2n-qubit vector of the
+    row-major rho (cpu.py:452-498): each gate's U on the row qubits q (bit 2n-q-1) and
+    conj(U) on the column qubits q + n (bit n-q-1), so the pair is rho -> U rho U^dagger."""
+    out = []
+    for kind, targets, controls, entries in lower(gates):
+        out.append((kind, targets, controls, entries))
+        out.append((kind, tuple(q + nqubits for q in targets), tuple(q + nqubits for q in controls),
+                    np.conj(entries)))
+    return out
 
-    def __init__(self, ctx: "_lib.Context", gates, nqubits: int, dtype: str = "complex128", tile_bits: int = 0):
+
+class FusedProgram:
+    """A circuit planned into fused passes for one state size and dtype (``ops``, when
+    given, replaces the lowering of ``gates``)."""
+
+    def __init__(self, ctx: "_lib.Context", gates, nqubits: int, dtype: str = "complex128", tile_bits: int = 0,
+                 ops: Optional[List[tuple]] = None):
         lib = ctx.lib
         self.ctx = ctx
         self.nqubits = int(nqubits)
         self.dtype = dtype
-        ops = lower(gates)
+        ops = lower(gates) if ops is None else ops
         arr = (GateOp * max(1, len(ops)))()
         self._keep = []
         for i, (kind, targets, controls, entries) in enumerate(ops):

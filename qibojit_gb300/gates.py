@@ -168,6 +168,52 @@ class FusedGate(Gate):
         self.gates.append(gate)
 
 
+class Channel:
+    """A noise channel sum_k c_k U_k with the attributes NumbaBackend.apply_channel reads
+    (cpu.py:400-415): ``coefficients``, one gate per coefficient in ``gates``,
+    ``coefficient_sum`` and ``_all_unitary_operators``."""
+
+    name = "channel"
+
+    def __init__(self, coefficients: Sequence[float], gates: Sequence[Gate]):
+        if len(coefficients) != len(gates):
+            raise ValueError("a channel needs one coefficient per gate")
+        self.coefficients = tuple(float(c) for c in coefficients)
+        self.gates = tuple(gates)
+        self.coefficient_sum = float(sum(self.coefficients))
+        if not 0.0 <= self.coefficient_sum <= 1.0 + 1e-12 or min(self.coefficients, default=0.0) < 0.0:
+            raise ValueError("channel coefficients must be probabilities summing to at most 1")
+        self._all_unitary_operators = True
+
+    @property
+    def qubits(self):
+        return tuple(sorted({q for g in self.gates for q in g.qubits}))
+
+    @property
+    def target_qubits(self):
+        return self.qubits
+
+
+class PauliNoiseChannel(Channel):
+    """X, Y and Z on ``q`` with probabilities px, py, pz (zero ones are left out)."""
+
+    name = "paulinoise"
+
+    def __init__(self, q: int, px: float = 0.0, py: float = 0.0, pz: float = 0.0):
+        pairs = [(p, cls(q)) for p, cls in ((px, X), (py, Y), (pz, Z)) if p > 0]
+        super().__init__([p for p, _ in pairs], [g for _, g in pairs])
+
+
+class UnitaryChannel(Channel):
+    """Unitary matrices on given qubits with given probabilities: ``ops`` is a list of
+    (qubits, matrix) pairs."""
+
+    name = "unitarychannel"
+
+    def __init__(self, probabilities: Sequence[float], ops: Sequence):
+        super().__init__(probabilities, [Unitary(np.asarray(m), *qs) for qs, m in ops])
+
+
 class Circuit:
     def __init__(self, nqubits: int):
         self.nqubits = int(nqubits)
