@@ -394,8 +394,8 @@ static void merge_signs(FOp* ops, int begin, int* end) {
   *end = w;
 }
 
-// Folds runs of register-only diagonals of a phase (one-bit diagonals on register
-// slots, sign diagonals without thread or tile bits) into one FOP_DIAGR table of 16
+// Folds runs of register-only diagonals of a phase (diagonals and sign diagonals whose
+// table bits and controls are all register bits) into one FOP_DIAGR table of 16
 // complex factors, one multiply per amplitude for the whole run.  These foldable
 // diagonals are first regrouped: each may sit anywhere between the mixing ops on its
 // own slots before and after it (it commutes with the rest, diagonals included), and
@@ -405,16 +405,12 @@ static void merge_signs(FOp* ops, int begin, int* end) {
 template <typename T>
 static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, int begin, int* end, int* ncoef,
                                     int* slack, std::vector<int32_t>* src) {
-  auto diag_slot = [](const FOp& f) -> int {  // register slot of a one-bit register diagonal, else -1
-    if (f.type != FOP_DIAG || f.nd != 1 || f.omask || f.tmask || f.jmask != 0xffffu || f.tb[0] >= 0 || f.ob[0] >= 0)
-      return -1;
-    for (int u = 0; u < kRB; u++) {
-      bool same = true;
-      for (int j = 0; j < 16; j++)
-        if ((int)((f.rpart >> (4 * j)) & 15) != ((j >> u) & 1)) same = false;
-      if (same) return u;
-    }
-    return -1;
+  // a diagonal whose table bits and controls are all register bits
+  auto reg_diag = [](const FOp& f) {
+    if (f.type != FOP_DIAG || f.omask || f.tmask) return false;
+    for (int i = 0; i < f.nd; i++)
+      if (f.tb[i] >= 0 || f.ob[i] >= 0) return false;
+    return true;
   };
   auto reg_sign = [](const FOp& f) {
     if (f.type != FOP_SIGN || f.omask || f.tmask) return false;
@@ -422,14 +418,20 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
       if (f.tb[i] >= 0 || f.ob[i] >= 0) return false;
     return true;
   };
+  auto rpart_of = [](const FOp& f, int j) { return (int)((f.rpart >> (4 * j)) & 15); };
   // register slots a foldable diagonal depends on
   auto fold_slots = [&](const FOp& f) -> unsigned {
-    const int u = diag_slot(f);
-    if (u >= 0) return 1u << u;
     unsigned m = 0;
     for (int v = 0; v < kRB; v++)
-      for (int j = 0; j < 16; j++)
-        if (((f.neg[0] >> j) & 1) != ((f.neg[0] >> (j ^ (1 << v))) & 1)) m |= 1u << v;
+      for (int j = 0; j < 16; j++) {
+        const int k = j ^ (1 << v);
+        if (reg_diag(f)) {
+          const bool a = (f.jmask >> j) & 1, b = (f.jmask >> k) & 1;
+          if (a != b || (a && rpart_of(f, j) != rpart_of(f, k))) m |= 1u << v;
+        } else if (((f.neg[0] >> j) & 1) != ((f.neg[0] >> k) & 1)) {
+          m |= 1u << v;
+        }
+      }
     return m;
   };
   // register slots whose diagonals a fixed op does not commute with (all 4: unknown kind)
@@ -451,7 +453,7 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
     std::vector<int> gap, lo, hi;  // per foldable: fixed ops before it, interval of gaps
     for (int r = begin; r < *end; r++) {
       const FOp& f = pp->ops[r];
-      if (diag_slot(f) >= 0 || reg_sign(f)) {
+      if (reg_diag(f) || reg_sign(f)) {
         fold.push_back(f);
         gap.push_back((int)fixed.size());
       } else {
@@ -491,12 +493,12 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
   }
   int w = begin;
   for (int r = begin; r < *end;) {
-    if (diag_slot(pp->ops[r]) < 0 && !reg_sign(pp->ops[r])) {
+    if (!reg_diag(pp->ops[r]) && !reg_sign(pp->ops[r])) {
       pp->ops[w++] = pp->ops[r++];
       continue;
     }
     int e = r, ndiag = 0;
-    while (e < *end && (diag_slot(pp->ops[e]) >= 0 || reg_sign(pp->ops[e]))) ndiag += diag_slot(pp->ops[e++]) >= 0;
+    while (e < *end && (reg_diag(pp->ops[e]) || reg_sign(pp->ops[e]))) ndiag += reg_diag(pp->ops[e++]);
     if (ndiag == 0 || e - r < 2 || *slack < 16) {
       while (r < e) pp->ops[w++] = pp->ops[r++];
       continue;
@@ -505,19 +507,18 @@ static void fold_register_diagonals(const sv_program* prog, PassParams<T>* pp, i
     for (int j = 0; j < 16; j++) tab[j] = 1.0;
     for (int q = r; q < e; q++) {
       const FOp& f = pp->ops[q];
-      const int u = diag_slot(f);
-      if (u < 0) {
+      if (!reg_diag(f)) {
         for (int j = 0; j < 16; j++)
           if ((f.neg[0] >> j) & 1) tab[j] = -tab[j];
         continue;
       }
-      std::complex<double> c[2];
-      for (int b = 0; b < 2; b++) {
-        const HostOp& h = prog->ops[(*src)[2 * (f.coef + b)]];
-        const int ent = (*src)[2 * (f.coef + b) + 1];
-        c[b] = std::complex<double>(h.m[2 * ent], h.m[2 * ent + 1]);
+      for (int j = 0; j < 16; j++) {
+        if (!((f.jmask >> j) & 1)) continue;  // register controls: the entry is 1 elsewhere
+        const int c = (int)f.coef + rpart_of(f, j);
+        const HostOp& h = prog->ops[(*src)[2 * c]];
+        const int ent = (*src)[2 * c + 1];
+        tab[j] *= std::complex<double>(h.m[2 * ent], h.m[2 * ent + 1]);
       }
-      for (int j = 0; j < 16; j++) tab[j] *= c[(j >> u) & 1];
     }
     FOp m;
     memset(&m, 0, sizeof(m));

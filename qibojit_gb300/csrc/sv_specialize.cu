@@ -201,19 +201,17 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
       if (dyn) o << "      sv::apply_negations(v, pn);\n      pn = 0;\n";
       dyn = false;
     };
-    for (int q = P.op_begin; q < P.op_end; q++) {
-      const FOp& f = p.ops[q];
+    // the thread / tile control test of an op, and the non-register part of a diagonal's
+    // table index (empty when the op has none)
+    auto cond_of = [](const FOp& f) {
       std::ostringstream c;
       if (f.type != FOP_D1RUN && f.type != FOP_D1RUNR && f.type != FOP_DIAGR) {
         if (f.omask) c << "((base & " << (long long)f.omask << "ll) == " << (long long)f.omask << "ll)";
         if (f.tmask) c << (f.omask ? " && " : "") << "((lbase & " << f.tmask << ") == " << f.tmask << ")";
       }
-      const std::string cond = c.str();
-      const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
-      if (f.type == FOP_D1RUN || f.type == FOP_D1RUNR || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R ||
-          f.type == FOP_DENSE1P || f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
-        flush();
-      // non-register part of a diagonal's table index
+      return c.str();
+    };
+    auto index_of = [](const FOp& f) {
       std::ostringstream te;
       bool tany = false;
       for (int i = 0; i < f.nd; i++) {
@@ -223,6 +221,28 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
         else continue;
         tany = true;
       }
+      return te.str();
+    };
+    // two diagonals whose factors depend on the registers in the same way
+    auto same_shape = [](const FOp& a, const FOp& b) {
+      if (a.jmask != b.jmask) return false;
+      for (int j = 0; j < 16; j++)
+        if (((a.jmask >> j) & 1) && ((a.rpart >> (4 * j)) & 15) != ((b.rpart >> (4 * j)) & 15)) return false;
+      return true;
+    };
+    std::vector<char> consumed(P.op_end, 0);
+    for (int q = P.op_begin; q < P.op_end; q++) {
+      const FOp& f = p.ops[q];
+      if (consumed[q]) continue;
+      const std::string cond = cond_of(f);
+      const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
+      if (f.type == FOP_D1RUN || f.type == FOP_D1RUNR || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R ||
+          f.type == FOP_DENSE1P || f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
+        flush();
+      const std::string tix = index_of(f);
+      const bool tany = !tix.empty();
+      std::ostringstream te;
+      te << tix;
       switch (f.type) {
         case FOP_D1RUN:
           for (int k = 0; k < f.nrun; k++)
@@ -269,15 +289,52 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
             dyn = true;
           }
           break;
-        case FOP_DIAG:
-          o << pre << "{\n        const int ti = " << (tany ? te.str() : std::string("0")) << ";\n        (void)ti;\n";
+        case FOP_DIAG: {
+          // this diagonal and the later ones of the same register shape up to the next
+          // non-diagonal op commute: their factors multiply per thread first (one complex
+          // multiply per distinct register index and op) and reach the amplitudes once
+          std::vector<int> members{q};
+          for (int q2 = q + 1; q2 < P.op_end && (p.ops[q2].type == FOP_DIAG || p.ops[q2].type == FOP_SIGN); q2++)
+            if (p.ops[q2].type == FOP_DIAG && same_shape(p.ops[q2], f)) {
+              members.push_back(q2);
+              consumed[q2] = 1;
+            }
+          if (members.size() == 1) {
+            o << pre << "{\n        const int ti = " << (tany ? te.str() : std::string("0")) << ";\n        (void)ti;\n";
+            for (int j = 0; j < 16; j++) {
+              if (!((f.jmask >> j) & 1)) continue;
+              const int r = (int)((f.rpart >> (4 * j)) & 15);
+              o << "        v[" << j << "] = sv::tmul(cf.c[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
+            }
+            o << "      }\n";
+            break;
+          }
+          std::vector<int> rs;  // distinct register parts of the table index
+          for (int j = 0; j < 16; j++) {
+            const int r = (int)((f.rpart >> (4 * j)) & 15);
+            if (((f.jmask >> j) & 1) && std::find(rs.begin(), rs.end(), r) == rs.end()) rs.push_back(r);
+          }
+          o << "      {  // " << members.size() << " diagonals of one register shape\n";
+          for (size_t k = 0; k < rs.size(); k++) o << "        T fr" << k << "{1, 0};\n";
+          for (int mq : members) {
+            const FOp& g = p.ops[mq];
+            const std::string gc = cond_of(g), gi = index_of(g);
+            o << "        " << (gc.empty() ? std::string() : "if (" + gc + ") ") << "{\n          const int ti = "
+              << (gi.empty() ? std::string("0") : gi) << ";\n          (void)ti;\n";
+            for (size_t k = 0; k < rs.size(); k++)
+              o << "          fr" << k << " = sv::tmul(cf.c[" << g.coef << " + (" << rs[k] << " | ti)], fr" << k
+                << ");\n";
+            o << "        }\n";
+          }
           for (int j = 0; j < 16; j++) {
             if (!((f.jmask >> j) & 1)) continue;
             const int r = (int)((f.rpart >> (4 * j)) & 15);
-            o << "        v[" << j << "] = sv::tmul(cf.c[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
+            const size_t k = std::find(rs.begin(), rs.end(), r) - rs.begin();
+            o << "        v[" << j << "] = sv::tmul(fr" << k << ", v[" << j << "]);\n";
           }
           o << "      }\n";
           break;
+        }
         default:
           return std::string();  // gradient markers and anything else: not specialisable
       }

@@ -80,7 +80,8 @@ def test_bad_tile_bits_are_rejected(lib):
 
 
 @pytest.mark.parametrize("dt", ["complex64", "complex128"])
-@pytest.mark.parametrize("circ", [random_circuit(12, 150, 7), circuits.brickwork(16, 6, 8)], ids=["random", "brickwork"])
+@pytest.mark.parametrize("circ", [random_circuit(12, 150, 7), circuits.brickwork(16, 6, 8), circuits.qft(14)],
+                         ids=["random", "brickwork", "qft"])
 def test_specialised_sources_compile(lib, circ, dt):
     """Phase folding, packing and code generation run, and NVRTC compiles every pass for
     sm_103a; without a GPU the call then stops at device selection."""
