@@ -95,3 +95,50 @@ def test_tfim_energy_dense_matches_hamiltonian_matrix(n):
         H -= 0.7 * op(X, i)
     x = random_state(n, 3)
     assert abs(tfim_energy_dense(x, n, 0.7) - np.real(np.vdot(x, H @ x))) < 1e-13
+
+
+def test_lower_density_is_u_rho_udagger():
+    """The 2n-qubit ops of a density-matrix program, applied densely to the row-major
+    rho, give U rho U^dagger (row qubit q = qubit q, column qubit q = qubit q + n)."""
+    from qibojit_gb300.fusion import lower_density
+
+    rng = np.random.default_rng(3)
+    n = 3
+    c = G.Circuit(n)
+    c.add([G.U3(0, *rng.uniform(0, 6, 3)), G.CNOT(2, 1), G.CU1(1, 0, theta=0.7), G.fSim(0, 2, 0.3, 0.4),
+           G.Y(1), G.FanOut(0, 1, 2)])
+    a = rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))
+    rho = a @ a.conj().T
+    vec = rho.reshape(-1)
+    ops = lower_density(c.queue, n)
+    assert len(ops) == 2 * len(lower(c.queue))
+    for kind, targets, controls, entries in ops:
+        k = len(targets)
+        m = np.diag(entries) if kind == SV_OP_DIAG else entries.reshape(2**k, 2**k)
+        vec = apply_dense(vec, m, list(targets), list(controls), 2 * n)
+    u = np.eye(8, dtype=complex)
+    for g in c.queue:
+        for t in (g.target_qubits if type(g).__name__ == "FanOut" else [None]):
+            if t is None:
+                cols = [apply_dense(u[:, j], g.base_matrix(), list(g.target_qubits), list(g.control_qubits), n)
+                        for j in range(8)]
+            else:
+                cols = [apply_dense(u[:, j], Matrices().X, [t], list(g.control_qubits), n) for j in range(8)]
+            u = np.stack(cols, axis=1)
+    np.testing.assert_allclose(vec.reshape(8, 8), u @ rho @ u.conj().T, atol=1e-12)
+
+
+def test_channels_expose_the_reference_attributes():
+    ch = G.PauliNoiseChannel(1, px=0.1, pz=0.25)
+    assert ch.coefficients == (0.1, 0.25) and [type(g).__name__ for g in ch.gates] == ["X", "Z"]
+    assert abs(ch.coefficient_sum - 0.35) < 1e-15 and ch._all_unitary_operators and ch.qubits == (1,)
+    u = G.UnitaryChannel([0.2, 0.3], [((0, 2), np.eye(4)), ((1,), np.eye(2))])
+    assert [g.target_qubits for g in u.gates] == [(0, 2), (1,)] and u.qubits == (0, 1, 2)
+    with pytest.raises(ValueError):
+        G.UnitaryChannel([0.7, 0.6], [((0,), np.eye(2)), ((1,), np.eye(2))])
+    with pytest.raises(ValueError):
+        G.Channel([0.1], [])
+    c = G.Circuit(3)
+    c.add(ch)
+    with pytest.raises(ValueError):
+        c.add(G.PauliNoiseChannel(3, px=0.1))
