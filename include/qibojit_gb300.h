@@ -259,6 +259,11 @@ int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubit
                     const int32_t* nops, int tile_bits, sv_batch** out);
 /* |0...0> then every circuit; asynchronous on the context stream. */
 int sv_batch_run(sv_context* ctx, sv_batch* b);
+/* Compiles one kernel per pass of every group with the group's structure as literals
+ * (as sv_program_specialize, on the unfolded plan: each circuit keeps its own
+ * coefficient block); later sv_batch_run calls launch them and record a new graph.
+ * Synchronises the device first.  SV_ERR_UNSUPPORTED when libnvrtc is absent. */
+int sv_batch_specialize(sv_context* ctx, sv_batch* b);
 /* Transverse-field Ising energies E_c = -sum_i <Z_i Z_{i+1}> - h sum_i <X_i> (open chain),
  * FP64 accumulation; `energies` (host) receives ncirc values; synchronises. */
 int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energies);

@@ -145,6 +145,13 @@ class BatchedCircuits:
     def run(self) -> None:
         _lib.check(self.lib.sv_batch_run(self.ctx.handle, self._h), "sv_batch_run")
 
+    def specialize(self) -> "BatchedCircuits":
+        """Compiles one pass kernel per group and pass with the group's structure as
+        literals (``sv_batch_specialize``: seconds, once per structure in the process);
+        later runs launch them."""
+        _lib.check(self.lib.sv_batch_specialize(self.ctx.handle, self._h), "sv_batch_specialize")
+        return self
+
     def tfim_energies(self, h: float = 1.0) -> np.ndarray:
         out = np.zeros(self.ncirc, dtype=np.float64)
         _lib.check(self.lib.sv_batch_tfim_energy(self.ctx.handle, self._h, float(h), out.ctypes.data),

@@ -1458,6 +1458,7 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
 
 int sv_program_destroy(sv_program* prog) {
   if (prog && prog->spec) specialized_free(prog->spec);
+  if (prog && prog->bspec) specialized_free(prog->bspec);
   delete prog;
   return SV_OK;
 }
@@ -1649,6 +1650,11 @@ static int batch_launches(Context* ctx, sv_batch* b) {
     args.coef_stride = (int64_t)prog->coef_total;
     args.ncirc = (int32_t)g.circuits.size();
     for (const Segment& s : prog->segments) {
+      if (prog->bspec) {
+        SV_TRY(specialized_launch_batched(ctx, prog, s.pass, st, g.d_states, g.d_coef, (int64_t)prog->coef_total,
+                                          args.ncirc));
+        continue;
+      }
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
       SV_TRY(launch_pass<T, true>(ctx, p, nullptr, threads, smem, p.ntiles * args.ncirc, st, args));
@@ -1668,7 +1674,7 @@ static void batch_free(sv_batch* b) {
   for (auto& g : b->groups) {
     if (g.d_coef) cudaFree(g.d_coef);
     if (g.d_states) cudaFree(g.d_states);
-    delete g.prog;
+    sv_program_destroy(g.prog);
   }
   for (int k = 0; k < kBatchStreams; k++) {
     if (b->streams[k]) cudaStreamDestroy(b->streams[k]);
@@ -1791,6 +1797,19 @@ int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubit
     return rc;
   }
   *out = b;
+  return SV_OK;
+}
+
+int sv_batch_specialize(sv_context* ctx, sv_batch* b) {
+  if (!ctx || !b) return set_error(SV_ERR_ARG, "null context or batch");
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  SV_TRY(check_cuda(cudaDeviceSynchronize(), "batch specialise sync"));
+  for (auto& g : b->groups) SV_TRY(specialize_batched(ctx, g.prog));
+  // the recorded graph holds the interpreting launches: record again on the next run
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
   return SV_OK;
 }
 

@@ -127,6 +127,8 @@ struct sv_program {
   bool pack_phases = false;
   // pass kernels compiled for this program's structure (sv_program_specialize), or null
   sv::Specialized* spec = nullptr;
+  // batched pass kernels for a group of circuits of this structure (sv_batch_specialize)
+  sv::Specialized* bspec = nullptr;
 };
 
 
@@ -143,6 +145,11 @@ inline size_t pass_smem(int kt) {
 int refold_program(sv_program* prog);
 // launches pass `pass` of a specialised program on the context stream
 int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state);
+// compiles the batched pass kernels of an (unfolded) program into prog->bspec
+int specialize_batched(Context* ctx, sv_program* prog);
+// launches batched pass `pass` over ncirc circuits: state pointer table, coefficient blocks
+int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, cudaStream_t stream, void* states,
+                               const void* coef, int64_t coef_stride, int ncirc);
 void specialized_free(Specialized* s);
 
 }  // namespace sv

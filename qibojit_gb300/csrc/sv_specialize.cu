@@ -123,9 +123,12 @@ KernelShape shape_of(int kt) {
   return k;
 }
 
-// CUDA source of one pass: kernel `name`, coefficients in a by-value parameter struct
+// CUDA source of one pass: kernel `name`, coefficients in a by-value parameter struct.
+// A batched pass (a group of circuits of one structure) runs over (circuit, tile) items
+// instead, with each circuit's state from a pointer table and its coefficients from its
+// block of a device array (coef_stride elements apart, the pass's own at coef_goff).
 template <typename T>
-std::string pass_source(const PassParams<T>& p, const char* name) {
+std::string pass_source(const PassParams<T>& p, const char* name, bool batched = false) {
   std::ostringstream o;
   const char* ty = sizeof(T) == 16 ? "sv::c128" : "sv::c64";
   const int kt = p.kt, n = p.n;
@@ -137,10 +140,15 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
   for (int g = 0; g < n; g++)
     if (std::find(tpos.begin(), tpos.end(), g) == tpos.end()) outer.push_back(g);
   const std::vector<int> low(tpos.begin(), tpos.begin() + (kt - kRB));
-  o << "struct " << name << "_coef { " << ty << " c[" << ncoef << "]; };\n"
-    << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
-    << "* __restrict__ state, const __grid_constant__ " << name << "_coef cf) {\n"
-    << "  using T = " << ty << ";\n"
+  const char* CF = batched ? "C" : "cf.c";  // where the ops read their coefficients
+  if (batched)
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
+      << "* const* __restrict__ states, const " << ty << "* __restrict__ coefs, long long coef_stride, int ncirc) {\n";
+  else
+    o << "struct " << name << "_coef { " << ty << " c[" << ncoef << "]; };\n"
+      << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
+      << "* __restrict__ state, const __grid_constant__ " << name << "_coef cf) {\n";
+  o << "  using T = " << ty << ";\n"
     << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n"
     << "  T* const buf0 = reinterpret_cast<T*>(smem_raw);\n"
     << "  constexpr int TSTRIDE = " << ((1 << kt) + (1 << (kt - kLowBits))) << ", SK = " << (nth + nth / 16) << ";\n"
@@ -155,28 +163,58 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
       if ((k >> i) & 1) d |= 1ll << tpos[kt - kRB + i];
     o << d << "ll" << (k < 15 ? ", " : "};\n");
   }
-  o << "  const long long nitems = " << p.ntiles << "ll;\n"
-    << "  auto origin = [&](long long t) -> long long { return " << deposit_expr("t", outer, true) << "; };\n"
-    << "  auto issue_load = [&](T* buf, long long base) {\n"
-    << "#pragma unroll\n"
-    << "    for (int k = 0; k < 16; k++)\n"
-    << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, state + (base | dtid | DEPK[k]));\n"
-    << "    sv::cp_async_commit();\n"
-    << "  };\n"
-    << "  long long t = blockIdx.x;\n"
-    << "  if (t < nitems) issue_load(buf0, origin(t));\n"
-    << "  int cur = 0;\n"
-    << "  for (; t < nitems; t += gridDim.x, cur ^= 1) {\n"
-    << "    T* const tile = buf0 + cur * TSTRIDE;\n"
-    << "    const long long base = origin(t);\n"
-    << "    const long long tn = t + gridDim.x;\n"
-    << "    if (tn < nitems) {\n"
-    << "      issue_load(buf0 + (cur ^ 1) * TSTRIDE, origin(tn));\n"
-    << "      sv::cp_async_wait<1>();\n"
-    << "    } else {\n"
-    << "      sv::cp_async_wait<0>();\n"
-    << "    }\n"
-    << "    __syncthreads();\n";
+  if (batched) {
+    const int tshift = n - kt;
+    o << "  const long long nitems = " << p.ntiles << "ll * ncirc;\n"
+      << "  auto origin = [&](long long it) -> long long { const long long t = it & " << (p.ntiles - 1) << "ll; return "
+      << deposit_expr("t", outer, true) << "; };\n"
+      << "  auto item_state = [&](long long it) -> T* { return states[it >> " << tshift << "]; };\n"
+      << "  auto issue_load = [&](T* buf, const T* sp, long long base) {\n"
+      << "#pragma unroll\n"
+      << "    for (int k = 0; k < 16; k++)\n"
+      << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, sp + (base | dtid | DEPK[k]));\n"
+      << "    sv::cp_async_commit();\n"
+      << "  };\n"
+      << "  long long t = blockIdx.x;\n"
+      << "  if (t < nitems) issue_load(buf0, item_state(t), origin(t));\n"
+      << "  int cur = 0;\n"
+      << "  for (; t < nitems; t += gridDim.x, cur ^= 1) {\n"
+      << "    T* const tile = buf0 + cur * TSTRIDE;\n"
+      << "    const long long base = origin(t);\n"
+      << "    T* const st = item_state(t);\n"
+      << "    const T* const C = coefs + (t >> " << tshift << ") * coef_stride + " << p.coef_goff << ";\n"
+      << "    const long long tn = t + gridDim.x;\n"
+      << "    if (tn < nitems) {\n"
+      << "      issue_load(buf0 + (cur ^ 1) * TSTRIDE, item_state(tn), origin(tn));\n"
+      << "      sv::cp_async_wait<1>();\n"
+      << "    } else {\n"
+      << "      sv::cp_async_wait<0>();\n"
+      << "    }\n"
+      << "    __syncthreads();\n";
+  } else {
+    o << "  const long long nitems = " << p.ntiles << "ll;\n"
+      << "  auto origin = [&](long long t) -> long long { return " << deposit_expr("t", outer, true) << "; };\n"
+      << "  auto issue_load = [&](T* buf, long long base) {\n"
+      << "#pragma unroll\n"
+      << "    for (int k = 0; k < 16; k++)\n"
+      << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, state + (base | dtid | DEPK[k]));\n"
+      << "    sv::cp_async_commit();\n"
+      << "  };\n"
+      << "  long long t = blockIdx.x;\n"
+      << "  if (t < nitems) issue_load(buf0, origin(t));\n"
+      << "  int cur = 0;\n"
+      << "  for (; t < nitems; t += gridDim.x, cur ^= 1) {\n"
+      << "    T* const tile = buf0 + cur * TSTRIDE;\n"
+      << "    const long long base = origin(t);\n"
+      << "    const long long tn = t + gridDim.x;\n"
+      << "    if (tn < nitems) {\n"
+      << "      issue_load(buf0 + (cur ^ 1) * TSTRIDE, origin(tn));\n"
+      << "      sv::cp_async_wait<1>();\n"
+      << "    } else {\n"
+      << "      sv::cp_async_wait<0>();\n"
+      << "    }\n"
+      << "    __syncthreads();\n";
+  }
   for (int ph = 0; ph < p.nphases; ph++) {
     const Phase& P = p.phases[ph];
     std::vector<int> nonreg;
@@ -246,25 +284,25 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
       switch (f.type) {
         case FOP_D1RUN:
           for (int k = 0; k < f.nrun; k++)
-            o << "      sv::dense1_regs<T, " << (int)f.ru[k] << ">(v, cf.c + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+            o << "      sv::dense1_regs<T, " << (int)f.ru[k] << ">(v, " << CF << " + " << (f.coef + 4 * k) << ", 0xffffu);\n";
           break;
         case FOP_D1RUNR:
           for (int k = 0; k < f.nrun; k++)
-            o << "      sv::dense1r_regs<T, " << (int)f.ru[k] << ">(v, cf.c + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+            o << "      sv::dense1r_regs<T, " << (int)f.ru[k] << ">(v, " << CF << " + " << (f.coef + 4 * k) << ", 0xffffu);\n";
           break;
         case FOP_DIAGR:  // commutes with the pending sign flips
           for (int j = 0; j < 16; j++)
-            o << "      v[" << j << "] = sv::tmul(cf.c[" << (f.coef + j) << "], v[" << j << "]);\n";
+            o << "      v[" << j << "] = sv::tmul(" << CF << "[" << (f.coef + j) << "], v[" << j << "]);\n";
           break;
         case FOP_DENSE1:
-          o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
+          o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, " << CF << " + " << f.coef << ", " << f.jmask << "u);\n";
           break;
         case FOP_DENSE1P:
-          o << pre << "sv::pivot1_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, cf.c + " << f.coef << ", "
+          o << pre << "sv::pivot1_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, " << CF << " + " << f.coef << ", "
             << f.jmask << "u);\n";
           break;
         case FOP_DENSE1R:
-          o << pre << "sv::dense1r_regs<T, " << (int)f.u0 << ">(v, cf.c + " << f.coef << ", " << f.jmask << "u);\n";
+          o << pre << "sv::dense1r_regs<T, " << (int)f.u0 << ">(v, " << CF << " + " << f.coef << ", " << f.jmask << "u);\n";
           break;
         case FOP_X1:
           o << pre << "sv::x1_regs<T, " << (int)f.u0 << ">(v, " << f.jmask << "u);\n";
@@ -274,7 +312,7 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
             << f.jmask << "u);\n";
           break;
         case FOP_DENSE2:
-          o << pre << "sv::dense2_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, cf.c + " << f.coef << ", "
+          o << pre << "sv::dense2_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, " << CF << " + " << f.coef << ", "
             << f.jmask << "u);\n";
           break;
         case FOP_SIGN:
@@ -304,7 +342,7 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
             for (int j = 0; j < 16; j++) {
               if (!((f.jmask >> j) & 1)) continue;
               const int r = (int)((f.rpart >> (4 * j)) & 15);
-              o << "        v[" << j << "] = sv::tmul(cf.c[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
+              o << "        v[" << j << "] = sv::tmul(" << CF << "[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
             }
             o << "      }\n";
             break;
@@ -322,7 +360,7 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
             o << "        " << (gc.empty() ? std::string() : "if (" + gc + ") ") << "{\n          const int ti = "
               << (gi.empty() ? std::string("0") : gi) << ";\n          (void)ti;\n";
             for (size_t k = 0; k < rs.size(); k++)
-              o << "          fr" << k << " = sv::tmul(cf.c[" << g.coef << " + (" << rs[k] << " | ti)], fr" << k
+              o << "          fr" << k << " = sv::tmul(" << CF << "[" << g.coef << " + (" << rs[k] << " | ti)], fr" << k
                 << ");\n";
             o << "        }\n";
           }
@@ -344,7 +382,8 @@ std::string pass_source(const PassParams<T>& p, const char* name) {
     o << "      __syncthreads();\n    }\n";
   }
   o << "#pragma unroll\n"
-    << "    for (int k = 0; k < 16; k++) sv::stg_stream(state + (base | dtid | DEPK[k]), tile[stid + k * SK]);\n"
+    << "    for (int k = 0; k < 16; k++) sv::stg_stream(" << (batched ? "st" : "state")
+    << " + (base | dtid | DEPK[k]), tile[stid + k * SK]);\n"
     << "    __syncthreads();  // this buffer is refilled by the prefetch two tiles later\n"
     << "  }\n}\n";
   return o.str();
@@ -401,18 +440,16 @@ struct Specialized {
 
 void specialized_free(Specialized* s) { delete s; }
 
+// generates, compiles (in parallel, through the process cache) and loads the pass
+// kernels of a program, single-state or batched
 template <typename T>
-static int specialize_typed(Context* ctx, sv_program* prog) {
-  if (!nvrtc().ok)
-    return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
-  // specialised passes run the phase-folded plan fastest (no op decoding to pay for)
-  SV_TRY(refold_program(prog));
+static int build_kernels(Context* ctx, const sv_program* prog, bool batched, std::unique_ptr<Specialized>* out) {
   const int np = prog->npasses;
-  std::vector<std::string> names(np), sources(np);
+  const char* name = batched ? "sv_bpass" : "sv_pass";
+  std::vector<std::string> sources(np);
   for (int i = 0; i < np; i++) {
     const PassParams<T>& p = *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)i * prog->pass_bytes);
-    names[i] = "sv_pass";
-    sources[i] = pass_source<T>(p, "sv_pass");
+    sources[i] = pass_source<T>(p, name, batched);
     if (sources[i].empty()) return set_error(SV_ERR_UNSUPPORTED, "pass %d holds ops that cannot be specialised", i);
   }
   // compile the sources not in the cache, in parallel
@@ -459,7 +496,7 @@ static int specialize_typed(Context* ctx, sv_program* prog) {
       CompiledKernel ck;
       SV_TRY(check_cuda(cudaLibraryLoadData(&ck.lib, cubins[k].data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
                         "cudaLibraryLoadData"));
-      SV_TRY(check_cuda(cudaLibraryGetKernel(&ck.kernel, ck.lib, names[todo[k]].c_str()), "cudaLibraryGetKernel"));
+      SV_TRY(check_cuda(cudaLibraryGetKernel(&ck.kernel, ck.lib, name), "cudaLibraryGetKernel"));
       cache()[sources[todo[k]]] = ck;
     }
   }
@@ -482,8 +519,47 @@ static int specialize_typed(Context* ctx, sv_program* prog) {
                       "specialised pass occupancy"));
     if (pk.per_sm < 1) return set_error(SV_ERR_ARG, "specialised pass %d does not fit on an SM", i);
   }
+  *out = std::move(s);
+  return SV_OK;
+}
+
+template <typename T>
+static int specialize_typed(Context* ctx, sv_program* prog) {
+  if (!nvrtc().ok)
+    return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
+  // specialised passes run the phase-folded plan fastest (no op decoding to pay for)
+  SV_TRY(refold_program(prog));
+  std::unique_ptr<Specialized> s;
+  SV_TRY(build_kernels<T>(ctx, prog, false, &s));
   if (prog->spec) specialized_free(prog->spec);
   prog->spec = s.release();
+  return SV_OK;
+}
+
+int specialize_batched(Context* ctx, sv_program* prog) {
+  if (!nvrtc().ok)
+    return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
+  // batched programs keep the unfolded plan: every circuit's coefficients are its own
+  // gates' entries, gathered through the plan's coefficient-source map
+  if (prog->fold_diagonals) return set_error(SV_ERR_ARG, "batched passes need an unfolded program");
+  std::unique_ptr<Specialized> s;
+  SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, true, &s) : build_kernels<c64>(ctx, prog, true, &s));
+  if (prog->bspec) specialized_free(prog->bspec);
+  prog->bspec = s.release();
+  return SV_OK;
+}
+
+int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, cudaStream_t stream, void* states,
+                               const void* coef, int64_t coef_stride, int ncirc) {
+  const PassKernel& pk = prog->bspec->passes[pass];
+  const int64_t items = ((int64_t)1 << (prog->nqubits - prog->kt)) * ncirc;
+  int64_t grid = (int64_t)pk.per_sm * ctx->num_sms;
+  if (grid > items) grid = items;
+  long long stride = (long long)coef_stride;
+  void* args[] = {&states, const_cast<void**>(&coef), &stride, &ncirc};
+  SV_TRY(check_cuda(cudaLaunchKernel((const void*)pk.kernel, dim3((unsigned)grid), dim3(pk.threads), args, pk.smem,
+                                     stream),
+                    "specialised batched pass launch"));
   return SV_OK;
 }
 

@@ -70,3 +70,36 @@ def test_batch_of_random_circuits(backend):
     for i, c in enumerate(circs):
         want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits), fuse=False))
         np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("dt,tol", [("complex128", 1e-12), ("complex64", 2e-5)])
+def test_specialised_batch_matches_single_circuits(backend, dt, tol):
+    """sv_batch_specialize: one compiled kernel per group and pass, every circuit's own
+    coefficients; states against the per-gate path, energies against the dense formula,
+    and the graph recorded after specialising replays the same energies."""
+    specs = hea_batch(48, seed=17, nmin=8, nmax=16, lmin=2, lmax=6)
+    circs = [hea_circuit(n, L, p) for n, L, p in specs]
+    batch = BatchedCircuits(backend, circs, dt)
+    batch.run()                      # interpreting kernels, graph recorded
+    e0 = batch.tfim_energies(1.0)
+    batch.specialize()
+    batch.run()                      # specialised, eager, new graph recorded
+    e1 = batch.tfim_energies(1.0)
+    for i, c in enumerate(circs):
+        got = backend.to_numpy(batch.state(i))
+        want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits, dtype=dt), fuse=False))
+        np.testing.assert_allclose(got, want, rtol=0, atol=tol)
+    np.testing.assert_allclose(e1, e0, atol=1e-11 if dt == "complex128" else 1e-4)
+    batch.run()                      # graph replay of the specialised launches
+    np.testing.assert_array_equal(batch.tfim_energies(1.0), e1)
+
+
+def test_specialised_batch_of_random_circuits(backend):
+    circs = [random_circuit(10 + (k % 2), 40, seed=300 + k % 2,
+                            families=["one", "one_p", "two_c", "two_p", "swap", "fsim", "u2q", "zc", "ccz", "toffoli"])
+             for k in range(6)]
+    batch = BatchedCircuits(backend, circs, "complex128").specialize()
+    batch.run()
+    for i, c in enumerate(circs):
+        want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits), fuse=False))
+        np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want, rtol=0, atol=1e-12)
