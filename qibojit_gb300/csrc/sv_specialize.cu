@@ -12,10 +12,14 @@
 // cudaLibraryLoadData and launched like the interpreted pass: same tiles, same
 // double-buffered cp.async staging, same register ops (sv_device.cuh, whose text is
 // compiled into this library).  Compiled kernels are cached per process by their
-// source text, which holds no coefficient values.
+// source text, which holds no coefficient values, and their cubins on disk.
 #include <dlfcn.h>
+#include <errno.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <condition_variable>
@@ -48,6 +52,7 @@ struct Nvrtc {
   nvrtcResult_t (*log)(nvrtcProgram_t, char*) = nullptr;
   nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t*) = nullptr;
   nvrtcResult_t (*cubin)(nvrtcProgram_t, char*) = nullptr;
+  nvrtcResult_t (*version)(int*, int*) = nullptr;
   bool ok = false;
 };
 
@@ -70,6 +75,7 @@ const Nvrtc& nvrtc() {
     api.log = (decltype(api.log))sym("nvrtcGetProgramLog");
     api.cubin_size = (decltype(api.cubin_size))sym("nvrtcGetCUBINSize");
     api.cubin = (decltype(api.cubin))sym("nvrtcGetCUBIN");
+    api.version = (decltype(api.version))sym("nvrtcVersion");
     api.ok = api.create && api.compile && api.destroy && api.log_size && api.log && api.cubin_size && api.cubin;
   });
   return api;
@@ -401,17 +407,104 @@ std::unordered_map<std::string, CompiledKernel>& cache() {
   return c;
 }
 
-// NVRTC: source -> cubin for sm_103a
+// ------------------------------------------------------------ on-disk cache
+// Compiled cubins are kept across processes in $QIBOJIT_GB300_CACHE (empty or "0":
+// off), else $XDG_CACHE_HOME/qibojit_gb300 or ~/.cache/qibojit_gb300.  A file holds
+// the full text it was compiled from (options, NVRTC version, header and kernel
+// source) and the cubin; it is used only when that text matches exactly and the cubin
+// is an ELF image.  Files are written to a temporary name and renamed into place, and
+// every disk error just means compiling again.
+const char* kCompileOpts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--diag-suppress=177"};
+constexpr int kNumCompileOpts = 3;
+
+std::string disk_cache_dir() {
+  const char* e = getenv("QIBOJIT_GB300_CACHE");
+  if (e) return (!*e || strcmp(e, "0") == 0) ? std::string() : std::string(e);
+  const char* x = getenv("XDG_CACHE_HOME");
+  if (x && *x) return std::string(x) + "/qibojit_gb300";
+  const char* h = getenv("HOME");
+  if (h && *h) return std::string(h) + "/.cache/qibojit_gb300";
+  return std::string();
+}
+
+uint64_t fnv1a64(const std::string& s) {
+  uint64_t h = 1469598103934665603ull;
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+bool make_dirs(const std::string& dir) {
+  for (size_t i = 1; i <= dir.size(); i++) {
+    if (i < dir.size() && dir[i] != '/') continue;
+    const std::string part = dir.substr(0, i);
+    if (mkdir(part.c_str(), 0755) != 0 && errno != EEXIST) return false;
+  }
+  return true;
+}
+
+const char kCacheMagic[8] = {'S', 'V', 'C', 'U', 'B', 'I', 'N', '1'};
+
+bool disk_load(const std::string& path, const std::string& key, std::vector<char>* cubin) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  bool ok = false;
+  char magic[8];
+  uint64_t klen = 0, clen = 0;
+  if (fread(magic, 1, 8, f) == 8 && memcmp(magic, kCacheMagic, 8) == 0 && fread(&klen, 8, 1, f) == 1 &&
+      klen == key.size()) {
+    std::string k(klen, '\0');
+    if (fread(&k[0], 1, klen, f) == klen && k == key && fread(&clen, 8, 1, f) == 1 && clen >= 4 &&
+        clen < (1ull << 31)) {
+      cubin->resize(clen);
+      ok = fread(cubin->data(), 1, clen, f) == clen && memcmp(cubin->data(), "\x7f" "ELF", 4) == 0;
+    }
+  }
+  fclose(f);
+  if (!ok) cubin->clear();
+  return ok;
+}
+
+void disk_store(const std::string& dir, const std::string& path, const std::string& key,
+                const std::vector<char>& cubin) {
+  if (!make_dirs(dir)) return;
+  const std::string tmp = path + ".tmp." + std::to_string((long long)getpid()) + "." +
+                          std::to_string((unsigned long long)std::hash<std::thread::id>()(std::this_thread::get_id()));
+  FILE* f = fopen(tmp.c_str(), "wb");
+  if (!f) return;
+  const uint64_t klen = key.size(), clen = cubin.size();
+  bool ok = fwrite(kCacheMagic, 1, 8, f) == 8 && fwrite(&klen, 8, 1, f) == 1 &&
+            fwrite(key.data(), 1, klen, f) == klen && fwrite(&clen, 8, 1, f) == 1 &&
+            fwrite(cubin.data(), 1, clen, f) == clen;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok || rename(tmp.c_str(), path.c_str()) != 0) unlink(tmp.c_str());
+}
+
+// NVRTC: source -> cubin for sm_103a (through the on-disk cache)
 int compile_cubin(const std::string& body, std::vector<char>* cubin, std::string* log) {
   const Nvrtc& api = nvrtc();
   const std::string src = std::string(kDeviceHeaderText) + "\n" + body;
+  const std::string dir = disk_cache_dir();
+  std::string key, path;
+  if (!dir.empty()) {
+    int major = 0, minor = 0;
+    if (api.version) api.version(&major, &minor);
+    key = "nvrtc " + std::to_string(major) + "." + std::to_string(minor);
+    for (int i = 0; i < kNumCompileOpts; i++) key += std::string(" ") + kCompileOpts[i];
+    key += "\n" + src;
+    char name[64];
+    snprintf(name, sizeof(name), "/%016llx_%zu.cubin", (unsigned long long)fnv1a64(key), key.size());
+    path = dir + name;
+    if (disk_load(path, key, cubin)) return SV_OK;
+  }
   nvrtcProgram_t prog = nullptr;
   if (api.create(&prog, src.c_str(), "sv_pass.cu", 0, nullptr, nullptr) != 0) {
     *log = "nvrtcCreateProgram failed";
     return SV_ERR_CUDA;
   }
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--diag-suppress=177"};
-  const int rc = api.compile(prog, 3, opts);
+  const int rc = api.compile(prog, kNumCompileOpts, kCompileOpts);
   size_t n = 0;
   api.log_size(prog, &n);
   log->assign(n, '\0');
@@ -423,6 +516,7 @@ int compile_cubin(const std::string& body, std::vector<char>* cubin, std::string
     api.cubin(prog, cubin->data());
   }
   api.destroy(&prog);
+  if (rc == 0 && !path.empty()) disk_store(dir, path, key, *cubin);
   return rc == 0 ? SV_OK : SV_ERR_CUDA;
 }
 

@@ -7,6 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# compiled pass kernels are not cached on disk during the tests (the cache test sets
+# its own directory); every test compiles what it runs
+os.environ["QIBOJIT_GB300_CACHE"] = "0"
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built engine library")

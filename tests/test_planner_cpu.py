@@ -95,3 +95,51 @@ def test_specialised_sources_compile(lib, circ, dt):
         assert rc == _lib.SV_ERR_CUDA and "cudaSetDevice" in msg, msg
     finally:
         lib.sv_program_destroy(h)
+
+
+def test_disk_cache_of_compiled_passes(lib, monkeypatch):
+    """NVRTC output goes to the on-disk cache: one file per distinct pass source, found
+    again (not rewritten) by a later specialisation of the same structure, and a damaged
+    file is replaced by a fresh compile."""
+    import glob
+    import os
+    import shutil
+
+    cache = os.path.join(os.path.dirname(_lib.__file__), "_build", "test_disk_cache")
+    shutil.rmtree(cache, ignore_errors=True)
+    monkeypatch.setenv("QIBOJIT_GB300_CACHE", cache)
+    circ = circuits.brickwork(14, 4, 3)
+
+    def specialise():
+        rc, h, ctx, _ = _create(lib, circ, "complex64", 10)
+        assert rc == _lib.SV_OK
+        try:
+            rc = lib.sv_program_specialize(ctypes.addressof(ctx), h)
+            msg = _lib.last_error()
+            if rc == _lib.SV_ERR_UNSUPPORTED:
+                pytest.skip(msg)
+            assert rc == _lib.SV_ERR_CUDA and "cudaSetDevice" in msg, msg
+        finally:
+            lib.sv_program_destroy(h)
+
+    try:
+        specialise()
+        files = sorted(glob.glob(os.path.join(cache, "*.cubin")))
+        assert files
+        for f in files:
+            data = open(f, "rb").read()
+            assert data[:8] == b"SVCUBIN1"
+            klen = int.from_bytes(data[8:16], "little")
+            clen = int.from_bytes(data[16 + klen:24 + klen], "little")
+            assert len(data) == 24 + klen + clen and data[24 + klen:28 + klen] == b"\x7fELF"
+        stamps = {f: os.stat(f).st_mtime_ns for f in files}
+        with open(files[0], "r+b") as fh:  # damage one cubin
+            fh.seek(-8, os.SEEK_END)
+            fh.truncate()
+        specialise()
+        again = sorted(glob.glob(os.path.join(cache, "*.cubin")))
+        assert again == files
+        assert [f for f in files if os.stat(f).st_mtime_ns != stamps[f]] == [files[0]]
+        assert not glob.glob(os.path.join(cache, "*.tmp.*"))
+    finally:
+        shutil.rmtree(cache, ignore_errors=True)
