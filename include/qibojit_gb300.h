@@ -247,6 +247,17 @@ int sv_program_destroy(sv_program* prog);
  * is absent. */
 int sv_program_specialize(sv_context* ctx, sv_program* prog);
 
+/* Introspection of a planned program, for tests that check the planner on the host:
+ * the host copy of pass `pass`'s parameter block (what the pass kernel receives) and
+ * its size, valid while the program lives. */
+int sv_program_pass_params(const sv_program* prog, int pass, const void** params, size_t* bytes);
+/* Byte layout of a pass block for `dtype` (SV_C128 / SV_C64): 32 entries, in order
+ * sizeof(block) and the offsets of n, kt, nphases, nops, ntiles, tile_pos, coef_goff,
+ * phases, ops, coef; sizeof(phase), offsets of rb, op_begin, op_end; sizeof(op), offsets
+ * of type, u0, u1, nd, tb, ob, jmask, tmask, coef, omask, rpart, neg, flags, nrun, ru;
+ * sizeof(coefficient). */
+int sv_pass_layout(int dtype, int64_t* offsets, int n);
+
 /* ---------------------------------------------------------- batched circuits */
 /* Many circuits of uneven size (8..34 qubits) in one job, for variational workloads
  * (the reference runs circuits one at a time through execute_circuit).  Circuits with

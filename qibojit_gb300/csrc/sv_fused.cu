@@ -28,6 +28,7 @@
 // This replaces the reference's fusion path (qibo Circuit.fuse -> FusedGate, applied
 // by qibojit as one dense 2^k x 2^k multi-qubit kernel, cpu.py:535-537,
 // gpu.py:929-930) with a schedule that needs no dense products of gate matrices.
+#include <stddef.h>
 #include <string.h>
 
 #include <algorithm>
@@ -1453,6 +1454,38 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
   if (nunfused) *nunfused = prog->nunfused;
   if (nfused_gates) *nfused_gates = prog->nfused_gates;
   if (tile_bits) *tile_bits = prog->kt;
+  return SV_OK;
+}
+
+int sv_program_pass_params(const sv_program* prog, int pass, const void** params, size_t* bytes) {
+  if (!prog || !params || !bytes) return set_error(SV_ERR_ARG, "null argument");
+  if (pass < 0 || pass >= prog->npasses) return set_error(SV_ERR_ARG, "pass %d out of range", pass);
+  *params = prog->passes.data() + (size_t)pass * prog->pass_bytes;
+  *bytes = prog->pass_bytes;
+  return SV_OK;
+}
+
+int sv_pass_layout(int dtype, int64_t* offsets, int n) {
+  if (!offsets || n < 32) return set_error(SV_ERR_ARG, "the layout has 32 entries");
+  if (dtype != SV_C128 && dtype != SV_C64) return set_error(SV_ERR_ARG, "pass blocks exist for complex dtypes");
+  auto fill = [&](auto tag) {
+    using P = decltype(tag);
+    const int64_t o[32] = {
+        (int64_t)sizeof(P), (int64_t)offsetof(P, n), (int64_t)offsetof(P, kt), (int64_t)offsetof(P, nphases),
+        (int64_t)offsetof(P, nops), (int64_t)offsetof(P, ntiles), (int64_t)offsetof(P, tile_pos),
+        (int64_t)offsetof(P, coef_goff), (int64_t)offsetof(P, phases), (int64_t)offsetof(P, ops),
+        (int64_t)offsetof(P, coef), (int64_t)sizeof(Phase), (int64_t)offsetof(Phase, rb),
+        (int64_t)offsetof(Phase, op_begin), (int64_t)offsetof(Phase, op_end), (int64_t)sizeof(FOp),
+        (int64_t)offsetof(FOp, type), (int64_t)offsetof(FOp, u0), (int64_t)offsetof(FOp, u1),
+        (int64_t)offsetof(FOp, nd), (int64_t)offsetof(FOp, tb), (int64_t)offsetof(FOp, ob),
+        (int64_t)offsetof(FOp, jmask), (int64_t)offsetof(FOp, tmask), (int64_t)offsetof(FOp, coef),
+        (int64_t)offsetof(FOp, omask), (int64_t)offsetof(FOp, rpart), (int64_t)offsetof(FOp, neg),
+        (int64_t)offsetof(FOp, flags), (int64_t)offsetof(FOp, nrun), (int64_t)offsetof(FOp, ru),
+        (int64_t)sizeof(P::coef[0])};
+    for (int i = 0; i < 32; i++) offsets[i] = o[i];
+  };
+  if (dtype == SV_C128) fill(PassParams<c128>{});
+  else fill(PassParams<c64>{});
   return SV_OK;
 }
 

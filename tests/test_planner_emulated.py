@@ -1,0 +1,93 @@
+"""The planner's output checked on the host: every pass block of a planned program is
+run by a numpy restatement of the tile kernel (``tests/pass_emulator.py``) and the
+result compared with the circuit applied gate by gate with dense matrices.  This
+covers the plans the GPU runs (complex128 phase-folded, complex64 unfolded, and the
+complex64 plan that specialisation re-folds: ``sv_program_specialize`` re-plans before
+it needs a device, so on this machine it stops at device selection with the folded
+plan in place) without a GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from qibojit_gb300 import _lib, circuits
+from qibojit_gb300 import gates as G
+from qibojit_gb300.matrices import Matrices
+from tests import pass_emulator as E
+from tests.circuits_random import random_circuit
+from tests.dense import apply_dense, random_state
+from tests.test_planner_cpu import _create
+
+FUSABLE = ["one", "one_p", "two_c", "two_p", "swap", "fsim", "gfsim", "toffoli", "ccz", "deutsch", "u1q", "u2q",
+           "cu1q", "cu2q", "fanout", "zc"]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def dense_reference(circ, state):
+    n = circ.nqubits
+    out = np.array(state, dtype=np.complex128)
+    for g in circ.queue:
+        if type(g).__name__ == "FanOut":
+            for t in g.target_qubits:
+                out = apply_dense(out, Matrices().X, [t], list(g.control_qubits), n)
+        elif type(g).__name__ == "Unitary":
+            out = apply_dense(out, g.parameters[0], list(g.target_qubits), list(g.control_qubits), n)
+        else:
+            out = apply_dense(out, g.base_matrix(), list(g.target_qubits), list(g.control_qubits), n)
+    return out
+
+
+def emulate(lib, circ, dt, tile_bits, refold=False):
+    rc, h, ctx, _ = _create(lib, circ, dt, tile_bits)
+    assert rc == _lib.SV_OK, _lib.last_error()
+    try:
+        if refold:
+            rc = lib.sv_program_specialize(ctypes.addressof(ctx), h)
+            if rc == _lib.SV_ERR_UNSUPPORTED:
+                pytest.skip(_lib.last_error())
+            assert rc == _lib.SV_ERR_CUDA
+        x = random_state(circ.nqubits, 11)
+        return x, E.run_program(lib, h, _lib.DTYPE_CODES[dt], x)
+    finally:
+        lib.sv_program_destroy(h)
+
+
+@pytest.mark.parametrize("dt,refold", [("complex128", False), ("complex64", False), ("complex64", True)],
+                         ids=["c128-folded", "c64", "c64-refolded"])
+@pytest.mark.parametrize("n,ngates,seed,tile_bits", [(9, 120, 1, 8), (10, 160, 2, 9), (12, 200, 3, 10),
+                                                     (12, 200, 4, 12), (13, 220, 5, 11)])
+def test_random_circuit_plans(lib, n, ngates, seed, tile_bits, dt, refold):
+    circ = random_circuit(n, ngates, seed, families=FUSABLE)
+    x, got = emulate(lib, circ, dt, tile_bits, refold)
+    want = dense_reference(circ, x)
+    np.testing.assert_allclose(got, want, atol=1e-11 if dt == "complex128" else 2e-5)
+
+
+@pytest.mark.parametrize("dt,refold", [("complex128", False), ("complex64", True)], ids=["c128", "c64-refolded"])
+@pytest.mark.parametrize("name", ["brickwork", "qft", "hea", "diagonal", "permutation"])
+def test_structured_circuit_plans(lib, name, dt, refold):
+    rng = np.random.default_rng(7)
+    if name == "brickwork":
+        circ = circuits.brickwork(12, 8, 3)
+    elif name == "qft":
+        circ = circuits.qft(11)
+    elif name == "hea":
+        circ = circuits.hea(11, 4)
+    elif name == "diagonal":
+        circ = G.Circuit(10)
+        for _ in range(80):
+            q = [int(v) for v in rng.permutation(10)]
+            circ.add([G.RZ(q[0], float(rng.uniform(0, 6))), G.CU1(q[1], q[2], float(rng.uniform(0, 6))),
+                      G.CZ(q[3], q[4]), G.CCZ(q[5], q[6], q[7])][int(rng.integers(4))])
+    else:
+        circ = G.Circuit(10)
+        for _ in range(80):
+            q = [int(v) for v in rng.permutation(10)]
+            circ.add([G.X(q[0]), G.CNOT(q[1], q[2]), G.SWAP(q[3], q[4]), G.TOFFOLI(q[5], q[6], q[7])][int(rng.integers(4))])
+    x, got = emulate(lib, circ, dt, 9, refold)
+    want = dense_reference(circ, x)
+    np.testing.assert_allclose(got, want, atol=1e-11 if dt == "complex128" else 2e-5)
