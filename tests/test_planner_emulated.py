@@ -91,3 +91,51 @@ def test_structured_circuit_plans(lib, name, dt, refold):
     x, got = emulate(lib, circ, dt, 9, refold)
     want = dense_reference(circ, x)
     np.testing.assert_allclose(got, want, atol=1e-11 if dt == "complex128" else 2e-5)
+
+
+class _HostContext:
+    """What FusedProgram reads from a context; the planner never dereferences it."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self._buf = ctypes.create_string_buffer(512)
+        self.handle = ctypes.addressof(self._buf)
+
+
+@pytest.mark.parametrize("dt", ["complex128", "complex64"])
+@pytest.mark.parametrize("n,ngates,seed", [(4, 40, 21), (5, 70, 22), (6, 90, 23)])
+def test_density_matrix_programs(lib, n, ngates, seed, dt):
+    """execute_circuit's density-matrix plan (lower_density: U on the rows, conj(U) on the
+    columns of the 2n-qubit vector of rho) gives U rho U^dagger."""
+    from qibojit_gb300.fusion import FusedProgram, lower_density
+
+    circ = random_circuit(n, ngates, seed, families=FUSABLE)
+    prog = FusedProgram(_HostContext(lib), circ.queue, 2 * n, dt, 0, ops=lower_density(circ.queue, n))
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((2**n, 2**n)) + 1j * rng.standard_normal((2**n, 2**n))
+    rho = a @ a.conj().T
+    rho /= np.trace(rho)
+    got = E.run_program(lib, prog._h, _lib.DTYPE_CODES[dt], rho.reshape(-1)).reshape(2**n, 2**n)
+    u = np.stack([dense_reference(circ, np.eye(2**n)[:, k]) for k in range(2**n)], axis=1)
+    np.testing.assert_allclose(got, u @ rho @ u.conj().T, atol=1e-11 if dt == "complex128" else 2e-5)
+
+
+def test_qibo_fused_gates_are_planned_as_their_parts(lib):
+    """A FusedGate (qibo's Circuit.fuse output) is lowered to its component gates."""
+    from qibojit_gb300.fusion import FusedProgram, matrix_fused
+
+    rng = np.random.default_rng(4)
+    n = 9
+    circ = G.Circuit(n)
+    ref = G.Circuit(n)
+    for k in range(12):
+        q = sorted(int(v) for v in rng.choice(n, 3, replace=False))
+        fg = G.FusedGate(*q)
+        for g in [G.U3(q[0], *rng.uniform(0, 6, 3)), G.CNOT(q[0], q[2]), G.RY(q[1], float(rng.uniform(0, 6))),
+                  G.CZ(q[1], q[2]), G.SWAP(q[0], q[1])]:
+            fg.append(g)
+        circ.add(fg)
+        ref.add(G.Unitary(matrix_fused(fg), *q))
+    prog = FusedProgram(_HostContext(lib), circ.queue, n, "complex128", 8)
+    x = random_state(n, 5)
+    np.testing.assert_allclose(E.run_program(lib, prog._h, _lib.SV_C128, x), dense_reference(ref, x), atol=1e-12)
