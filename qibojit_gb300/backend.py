@@ -1,11 +1,12 @@
 """``GB300Backend``: qibojit's backend API on the GB300 engine.
 
 The class mirrors the methods qibojit's ``NumbaBackend`` / ``CupyBackend`` expose
-for state vectors (``src/qibojit/backends/cpu.py:39-635``,
-``src/qibojit/backends/gpu.py:44-1076``): ``apply_gate`` and the
-``_one/_two/_multi_qubit_base`` kernels it dispatches to, ``zero_state``,
-``collapse_state``, ``calculate_probabilities``, ``sample_frequencies`` and
-``measure_frequencies_op``, plus the dtype/device/seed/thread setters.  Every
+(``src/qibojit/backends/cpu.py:39-635``, ``src/qibojit/backends/gpu.py:44-1076``):
+``apply_gate`` and the ``_one/_two/_multi_qubit_base`` kernels it dispatches to,
+``apply_channel``, ``zero_state``, ``collapse_state``, ``calculate_probabilities``,
+``sample_frequencies`` and ``measure_frequencies_op`` for state vectors and density
+matrices, plus the dtype/device/seed/thread setters; ``execute_circuit`` runs fused
+passes and ``execute_circuit_stream`` pipelines host states through them.  Every
 amplitude operation is one call through the C ABI into the CUDA library; there is
 no CPU path.  Device arrays are torch CUDA tensors (any contiguous CUDA tensor of
 the backend's dtype works), used only as memory.
@@ -88,6 +89,15 @@ def _is_channel(gate) -> bool:
     """A qibo noise channel as NumbaBackend.apply_channel consumes it (cpu.py:400-415):
     coefficients with one gate each."""
     return hasattr(gate, "coefficients") and hasattr(gate, "gates")
+
+
+def _inverse_target_matrix(gate, backend) -> np.ndarray:
+    """U^-1 on a gate's targets, its controls kept: the target block (controls all 1,
+    controls first) of the inverse of the gate's matrix.  The reference inverts the
+    whole matrix (cpu.py:461-464), which is the same for uncontrolled gates."""
+    full = np.linalg.inv(np.asarray(gate.matrix(backend), dtype=np.complex128))
+    d = 1 << len(gate.target_qubits)
+    return np.ascontiguousarray(full[-d:, -d:])
 
 
 def _dtype_name(x) -> str:
@@ -280,12 +290,10 @@ class GB300Backend(_QiboBackend):
                 flat = self._one_qubit_base(flat, n2, t + nqubits, "apply_x", x, q)
             return flat.reshape(shape)
         if inverse:
-            u = np.linalg.inv(np.asarray(gate.matrix(self)))
-            matrix = u if len(gate.control_qubits) == 0 else None
-            if matrix is None:
-                raise NotImplementedError("inverse of a controlled gate on a density matrix")
-            gate = type("Inverse", (), {"target_qubits": gate.target_qubits, "control_qubits": (),
-                                         "parameters": (), "name": "inverse"})()
+            matrix = _inverse_target_matrix(gate, self)
+            gate = type("Inverse", (), {"target_qubits": tuple(gate.target_qubits),
+                                         "control_qubits": tuple(gate.control_qubits),
+                                         "parameters": (matrix,), "name": "inverse"})()
             name = "Unitary"
         else:
             matrix = self._as_custom_matrix(gate, dtype)

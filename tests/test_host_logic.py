@@ -142,3 +142,20 @@ def test_channels_expose_the_reference_attributes():
     c.add(ch)
     with pytest.raises(ValueError):
         c.add(G.PauliNoiseChannel(3, px=0.1))
+
+
+@pytest.mark.parametrize("gate", [G.RX(0, 0.3), G.U3(1, 0.1, 0.2, 0.3), G.CU1(0, 1, 0.7), G.CRX(2, 0, 0.4),
+                                  G.TOFFOLI(0, 1, 2), G.CCZ(2, 1, 0), G.fSim(0, 1, 0.2, 0.5), G.CU3(1, 2, 0.3, 0.2, 0.1)],
+                         ids=lambda g: type(g).__name__)
+def test_inverse_target_matrix(gate):
+    """The inverse a density-matrix gate applies with inverse=True: controls kept, the
+    target block inverted."""
+    from qibojit_gb300.backend import _inverse_target_matrix
+
+    u = gate.base_matrix()
+    inv = _inverse_target_matrix(gate, None)
+    np.testing.assert_allclose(inv @ u, np.eye(u.shape[0]), atol=1e-14)
+    full = gate.matrix()
+    controlled_inv = np.eye(full.shape[0], dtype=complex)
+    controlled_inv[-u.shape[0]:, -u.shape[0]:] = inv
+    np.testing.assert_allclose(controlled_inv, np.linalg.inv(full), atol=1e-14)
