@@ -126,7 +126,10 @@ int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits,
  * exits; a call whose reduction would need more (more than 4094 partial sums, i.e.
  * a GPU with more than 511 SMs) is rejected with SV_ERR_ARG.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress) with the
- * device current, so make that first call before any stream capture.  All calls
+ * device current, so make that first call before any stream capture.  The address is
+ * kept for the life of the process: it does not survive cudaDeviceReset or any other
+ * teardown of the device's primary context, after which this entry point must not be
+ * called again in that process.  All calls
  * share the array and it keeps the last call's contents (every call overwrites what
  * it reads, nothing needs to start at zero); calls that overlap on the GPU (different
  * streams, or different host threads on one device) race on it.

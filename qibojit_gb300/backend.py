@@ -635,6 +635,17 @@ class GB300Backend(_QiboBackend):
         tdt = _torch_dtype(dtype)
         dev = [torch.empty(1 << n, dtype=tdt, device=self._tdevice) for _ in range(min(2, k_total))]
         up, comp, down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        # The device buffers come from the caching allocator on the caller's current
+        # stream, and earlier engine work sits on the context's own stream (the legacy
+        # default stream, which does not order against non-blocking streams): finish the
+        # latter and order the new streams after the former before touching anything.
+        cur = torch.cuda.current_stream(self._tdevice)
+        self.ctx.sync()
+        up.wait_stream(cur)
+        comp.wait_stream(cur)
+        for buf in dev:
+            for st in (up, comp, down):
+                buf.record_stream(st)
         freed = [None] * len(dev)
         self.ctx.set_stream(comp.cuda_stream)
         try:
@@ -658,6 +669,7 @@ class GB300Backend(_QiboBackend):
         finally:
             for st in (up, comp, down):
                 st.synchronize()
+            cur.wait_stream(down)
             self.ctx.set_stream(0)
         return host_outputs
 

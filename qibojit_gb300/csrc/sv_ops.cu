@@ -458,6 +458,36 @@ static int zero_state_impl(Context* ctx, void* state, int dtype, int nqubits) {
   return SV_OK;
 }
 
+// Measured qubits and outcome of a collapse call (both collapse entry points): the
+// reference maps qubit q to bit n-q-1 (cpu.py:548-552); bit j of `result`, counting
+// from the most significant, is the outcome of qubits[j].  Positions are stored in
+// ascending order with their outcome bits.
+static int decode_measured(int nqubits, const int32_t* qubits, int nq, int64_t result, Measured* out) {
+  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "collapse needs 1..n measured qubits");
+  if (result < 0 || result >= ((int64_t)1 << nq))
+    return set_error(SV_ERR_ARG, "outcome %lld out of range for %d qubits", (long long)result, nq);
+  Measured m;
+  memset(&m, 0, sizeof(m));
+  m.n = nq;
+  for (int j = 0; j < nq; j++) {
+    if (qubits[j] < 0 || qubits[j] >= nqubits)
+      return set_error(SV_ERR_ARG, "measured qubit %d out of range", qubits[j]);
+    const int pos = nqubits - qubits[j] - 1;
+    if (m.mask & ((int64_t)1 << pos)) return set_error(SV_ERR_ARG, "duplicate measured qubit %d", qubits[j]);
+    m.mask |= (int64_t)1 << pos;
+    if ((result >> (nq - 1 - j)) & 1) m.value |= (int64_t)1 << pos;
+  }
+  int k = 0;
+  for (int p = 0; p < nqubits; p++) {
+    if (!(m.mask & ((int64_t)1 << p))) continue;
+    m.pos[k] = p;
+    m.bit[k] = (int)((m.value >> p) & 1);
+    k++;
+  }
+  *out = m;
+  return SV_OK;
+}
+
 template <typename T>
 static int collapse_typed(Context* ctx, void* state, int nqubits, const Measured& m, int normalize) {
   const int64_t n = (int64_t)1 << nqubits;
@@ -815,29 +845,8 @@ int sv_collapse_state(sv_context* ctx, void* state, int dtype, int nqubits, cons
                       int nq, int64_t result, int normalize) {
   if (!ctx) return set_error(SV_ERR_ARG, "null context");
   SV_TRY(check_state(state, dtype, nqubits));
-  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "collapse needs 1..n measured qubits");
-  if (result < 0 || result >= ((int64_t)1 << nq))
-    return set_error(SV_ERR_ARG, "outcome %lld out of range for %d qubits", (long long)result, nq);
   Measured m;
-  memset(&m, 0, sizeof(m));
-  m.n = nq;
-  std::vector<std::pair<int, int>> pb;
-  for (int j = 0; j < nq; j++) {
-    if (qubits[j] < 0 || qubits[j] >= nqubits)
-      return set_error(SV_ERR_ARG, "measured qubit %d out of range", qubits[j]);
-    const int pos = nqubits - qubits[j] - 1;
-    const int bit = (int)((result >> (nq - 1 - j)) & 1);
-    for (auto& e : pb)
-      if (e.first == pos) return set_error(SV_ERR_ARG, "duplicate measured qubit %d", qubits[j]);
-    pb.push_back({pos, bit});
-    m.mask |= (int64_t)1 << pos;
-    if (bit) m.value |= (int64_t)1 << pos;
-  }
-  std::sort(pb.begin(), pb.end());
-  for (int j = 0; j < nq; j++) {
-    m.pos[j] = pb[j].first;
-    m.bit[j] = pb[j].second;
-  }
+  SV_TRY(decode_measured(nqubits, qubits, nq, result, &m));
   switch (dtype) {
     case SV_C128: return collapse_typed<c128>(ctx, state, nqubits, m, normalize);
     case SV_C64: return collapse_typed<c64>(ctx, state, nqubits, m, normalize);
@@ -897,9 +906,10 @@ int sv_measure_frequencies(sv_context* ctx, int64_t* frequencies, const void* pr
 // which every GPU that loads this library holds until the process exits.
 #include <mutex>
 
+#include "sv_noalloc_grid.h"
+
 namespace sv {
 
-constexpr int kNoAllocScratchDoubles = 4096;  // 32 KiB: norm partials + (norm^2, 1/norm)
 constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_collapse_scratch[kNoAllocScratchDoubles];
@@ -936,11 +946,7 @@ template <typename T>
 static int collapse_noalloc_typed(cudaStream_t stream, const NoAllocDevice& d, void* state, int nqubits,
                                   const Measured& m, int normalize) {
   const int64_t n = (int64_t)1 << nqubits;
-  const int64_t cap = (int64_t)d.num_sms * 8;
-  auto grid_of = [cap](int64_t work) {
-    int64_t g = (work + kOpsBlock - 1) / kOpsBlock;
-    return (unsigned)(g > cap ? cap : (g < 1 ? 1 : g));
-  };
+  auto grid_of = [&d](int64_t work) { return noalloc_grid(work, d.num_sms, kOpsBlock); };
   if (!normalize) {
     k_collapse_apply<T, false><<<grid_of(n), kOpsBlock, 0, stream>>>((T*)state, n, m.mask, m.value, nullptr);
     SV_LAUNCH_CHECK("no-alloc collapse launch");
@@ -950,7 +956,7 @@ static int collapse_noalloc_typed(cudaStream_t stream, const NoAllocDevice& d, v
   const unsigned grid = grid_of(nkept);
   // every block writes its own partial and the finish kernel writes both results
   // before the apply pass reads them, so nothing left from an earlier call is read
-  if ((int64_t)grid + 2 > kNoAllocScratchDoubles)
+  if (!noalloc_norm_fits(grid))
     return set_error(SV_ERR_ARG,
                      "no-alloc collapse needs %u doubles of scratch; its static array holds at most %d",
                      grid + 2, kNoAllocScratchDoubles);
@@ -971,28 +977,8 @@ extern "C" int sv_collapse_state_noalloc(void* stream, void* state, int dtype, i
                                          const int32_t* qubits, int nq, int64_t result, int normalize) {
   using namespace sv;
   SV_TRY(check_state(state, dtype, nqubits));
-  if (!qubits || nq < 1 || nq > nqubits) return set_error(SV_ERR_ARG, "collapse needs 1..n measured qubits");
-  if (result < 0 || result >= ((int64_t)1 << nq))
-    return set_error(SV_ERR_ARG, "outcome %lld out of range for %d qubits", (long long)result, nq);
   Measured m;
-  memset(&m, 0, sizeof(m));
-  m.n = nq;
-  for (int j = 0; j < nq; j++) {
-    if (qubits[j] < 0 || qubits[j] >= nqubits)
-      return set_error(SV_ERR_ARG, "measured qubit %d out of range", qubits[j]);
-    const int pos = nqubits - qubits[j] - 1;
-    if (m.mask & ((int64_t)1 << pos)) return set_error(SV_ERR_ARG, "duplicate measured qubit %d", qubits[j]);
-    m.mask |= (int64_t)1 << pos;
-    if ((result >> (nq - 1 - j)) & 1) m.value |= (int64_t)1 << pos;
-  }
-  // measured positions in ascending order, each with its outcome bit
-  int k = 0;
-  for (int p = 0; p < nqubits; p++) {
-    if (!(m.mask & ((int64_t)1 << p))) continue;
-    m.pos[k] = p;
-    m.bit[k] = (int)((m.value >> p) & 1);
-    k++;
-  }
+  SV_TRY(decode_measured(nqubits, qubits, nq, result, &m));
   int device = 0;
   SV_TRY(check_cuda(cudaGetDevice(&device), "cudaGetDevice"));
   if (device < 0 || device >= kNoAllocMaxDevices)

@@ -42,6 +42,22 @@ def _target_matrix(gate) -> np.ndarray:
     return np.asarray(attr(*gate.parameters) if callable(attr) else attr, dtype=np.complex128)
 
 
+def _expand(gates: Iterable) -> List:
+    """Component gates in application order: nested FusedGates flattened and a FanOut
+    written as one CNOT per target (its target matrix is the X of each CNOT)."""
+    from . import gates as G
+
+    out = []
+    for g in gates:
+        if type(g).__name__ == "FusedGate":
+            out.extend(_expand(g.gates))
+        elif getattr(g, "name", "") == "fanout":
+            out.extend(G.CNOT(g.control_qubits[0], t) for t in g.target_qubits)
+        else:
+            out.append(g)
+    return out
+
+
 def lower(gates: Iterable) -> List[tuple]:
     """Gates -> (kind, targets, controls, complex entries) in application order."""
     out = []
@@ -157,7 +173,7 @@ def matrix_fused(gate, dtype: str = "complex128") -> np.ndarray:
     qubits = list(gate.target_qubits)
     k = len(qubits)
     u = np.eye(2**k, dtype=np.complex128)
-    for g in gate.gates:
+    for g in _expand(gate.gates):
         m = _target_matrix(g)
         gq = list(g.control_qubits) + list(g.target_qubits)
         nc = len(g.control_qubits)

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs in a container that holds the qibojit sources (default location
-``/root/reference``, override with ``QIBOJIT_SRC``); the GPU machine only reads the
-committed ``.npz`` files.  numba is not installed there, so a stand-in module with
+Runs where the qibojit sources are available: pass the folder that holds the
+``qibojit`` package (the reference's ``src`` folder) as the first argument or in
+``QIBOJIT_SRC``; the GPU machine only reads the committed ``.npz`` files.  numba is not installed there, so a stand-in module with
 ``njit`` = identity and ``prange`` = ``range`` is placed in ``sys.modules`` first:
 this is the reference CI's own ``NUMBA_DISABLE_JIT=1`` mode
 (``pyproject.toml:55``), in which the kernels of
@@ -11,7 +11,7 @@ this is the reference CI's own ``NUMBA_DISABLE_JIT=1`` mode
 The base-method arithmetic (bit position m = n-q-1, ``nstates``, ``swap_targets``,
 the multi-target operand) follows ``src/qibojit/backends/cpu.py:565-635``; the case
 lists follow the parametrisations of ``tests/test_gates.py`` and
-``tests/test_ops.py``.  Usage: ``python tests/golden/make_golden.py``.
+``tests/test_ops.py``.  Usage: ``python tests/golden/make_golden.py <qibojit src folder>``.
 """
 from __future__ import annotations
 
@@ -23,7 +23,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.environ.get("QIBOJIT_SRC", "/root/reference/src")
+SRC = None  # set by main() from the command line or QIBOJIT_SRC
 
 
 def _load_reference():
@@ -209,4 +209,7 @@ def main():
 
 
 if __name__ == "__main__":
+    SRC = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QIBOJIT_SRC")
+    if not SRC or not os.path.isdir(os.path.join(SRC, "qibojit")):
+        sys.exit("usage: make_golden.py <folder holding the qibojit package> (or set QIBOJIT_SRC)")
     main()

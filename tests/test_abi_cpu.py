@@ -81,3 +81,37 @@ def test_int32_array():
     a, n = _lib.int32_array([3, 1, 2])
     assert n == 3 and list(a) == [3, 1, 2]
     assert _lib.int32_array([]) == (None, 0)
+
+
+def test_noalloc_grid_rule(tmp_path):
+    """The launch-size rule of sv_collapse_state_noalloc (csrc/sv_noalloc_grid.h),
+    compiled with the host compiler: a reduction fits the static array up to 4094
+    partials (one per block, capped at 8 blocks per SM), so any GPU of up to 511 SMs
+    is accepted and a 512-SM one would be rejected."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    src = tmp_path / "grid.cpp"
+    src.write_text(
+        '#include <stdio.h>\n#include "sv_noalloc_grid.h"\n'
+        "int main() {\n"
+        "  const long long works[] = {1, 255, 256, 257, 1LL << 20, 1LL << 30, 1LL << 36};\n"
+        "  const int sms[] = {1, 152, 511, 512, 1000};\n"
+        "  for (int s : sms) for (long long w : works) {\n"
+        "    unsigned g = sv::noalloc_grid(w, s, 256);\n"
+        "    printf(\"%d %lld %u %d\\n\", s, w, g, (int)sv::noalloc_norm_fits(g));\n"
+        "  }\n  return 0;\n}\n")
+    exe = tmp_path / "grid"
+    import subprocess
+
+    subprocess.run([cxx, "-std=c++17", "-I", os.path.join(ROOT, "qibojit_gb300", "csrc"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    for line in filter(None, out):
+        s, w, g, fits = (int(v) for v in line.split())
+        want = max(1, min((w + 255) // 256, 8 * s))
+        assert g == want
+        assert fits == (g + 2 <= 4096)
+        if s <= 511:
+            assert fits
+    assert any(line.split()[3] == "0" for line in out if line and line.split()[0] == "512")

@@ -241,3 +241,31 @@ def test_density_circuit_with_channels_vs_oracle(backend):
             O.apply_gate_density_matrix(ob, ref, n, t, c, "apply_two_qubit_gate", u)
     np.testing.assert_allclose(got, ref, atol=1e-12)
     assert abs(np.trace(got) - 1) < 1e-12
+
+
+# ------------------------------------------------------------------- inverse gates
+@pytest.mark.parametrize("gatename,qubits,params", [("CNOT", (0, 2), {}), ("CU3", (3, 1), {"theta": 0.3, "phi": 1.1,
+                                                                                          "lam": -0.4}),
+                                                    ("TOFFOLI", (0, 3, 1), {}), ("fSim", (2, 0), {"theta": 0.7,
+                                                                                                "phi": 0.2}),
+                                                    ("CRY", (1, 2), {"theta": 2.1}), ("CU1", (3, 0), {"theta": 0.9})])
+def test_inverse_gate_restores_density_matrix(backend, gatename, qubits, params, dtype):
+    """apply_gate then apply_gate(..., inverse=True) on a density matrix gives rho
+    back: controls kept, the target block inverted, and for complex64 the complex128
+    inverse operand cast down (U^-1 rho U after U rho U^dagger)."""
+    from qibojit_gb300 import gates
+
+    from tests.conftest import PARITY_ATOL
+
+    n = 4
+    rho = random_density_matrix(n, 41).astype(dtype)
+    backend.set_dtype(dtype)
+    gate = getattr(gates, gatename)(*qubits, **params)
+    state = backend.cast(rho, copy=True)
+    state = backend.apply_gate(gate, state, n)
+    moved = backend.to_numpy(state).copy()
+    state = backend.apply_gate(gate, state, n, inverse=True)
+    got = backend.to_numpy(state)
+    assert np.abs(moved - rho).max() > 1e-3  # the gate did act
+    tol = 10 * PARITY_ATOL[dtype]
+    np.testing.assert_allclose(got, rho, rtol=0, atol=tol)

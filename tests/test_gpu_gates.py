@@ -48,9 +48,59 @@ def test_kernels_match_reference_outputs(backend, case):
     else:
         got = _run(backend, lambda s: backend._multi_qubit_base(s, n, targets, gate, q), state)
     tol = PARITY_ATOL[str(state.dtype)]
-    # relative to the operand scale: fixtures use un-normalised random matrices
-    scale = max(1.0, float(np.abs(gate).max()) * (2 ** len(targets)))
-    np.testing.assert_allclose(got, case["out"], rtol=0, atol=tol * scale)
+    np.testing.assert_allclose(got, case["out"], rtol=0, atol=tol * _rounding_scale(case))
+
+
+def _oracle_apply(case, state, gate):
+    """The C oracle's kernel of a golden case on (state, gate)."""
+    ob = O.OracleBackend()
+    n, q, kernel = case["nqubits"], case["qubits"], case["kernel"]
+    targets = [int(t) for t in case["targets"]]
+    s = np.array(state, copy=True)
+    if case["family"] == "one":
+        return ob._one_qubit_base(s, n, targets[0], kernel, gate, q)
+    if case["family"] == "two":
+        return ob._two_qubit_base(s, n, targets[0], targets[1], kernel, gate, q)
+    return ob._multi_qubit_base(s, n, targets, gate, q)
+
+
+def _rounding_scale(case):
+    """max(1, max over outputs of sum_j |g_ij| |x_j|): the magnitude that floating-point
+    rounding of a gate row's dot product is proportional to.  The fixtures use
+    un-normalised random operands (as the reference's tests do), whose outputs reach
+    a few units; the absolute bar is applied relative to this scale."""
+    gate = case["gate"]
+    if gate is None or case["kernel"] in ("apply_x", "apply_y", "apply_z", "apply_swap"):
+        return 1.0
+    a = _oracle_apply(case, np.abs(case["state"]).astype(np.complex128), np.abs(gate).astype(np.complex128))
+    return max(1.0, float(np.abs(a).max()))
+
+
+UNITARY_CASES = [c for c in GOLDEN if c["kernel"] in ("apply_gate", "apply_two_qubit_gate", "apply_multi_qubit_gate")
+                 or c["family"] == "multi"]
+
+
+@pytest.mark.parametrize("case", UNITARY_CASES, ids=lambda c: c["id"])
+def test_kernels_match_oracle_unitary_operands_unscaled(backend, case):
+    """Every golden placement again with a normalised state and a random unitary
+    operand, against the C oracle at the unscaled bar (complex128 1e-12, complex64
+    1e-5 max-abs)."""
+    n = case["nqubits"]
+    targets = [int(t) for t in case["targets"]]
+    dtype = str(case["state"].dtype)
+    k = len(targets)
+    gate = random_unitary(2**k, 1000 + len(case["id"]) + n).astype(dtype)
+    state = random_state(n, 2000 + n + k, dtype)
+    q = case["qubits"]
+    if case["family"] == "one":
+        got = _run(backend, lambda s: backend._one_qubit_base(s, n, targets[0], case["kernel"], gate, q), state)
+    elif case["family"] == "two":
+        got = _run(backend, lambda s: backend._two_qubit_base(s, n, targets[0], targets[1], case["kernel"], gate, q),
+                   state)
+    else:
+        got = _run(backend, lambda s: backend._multi_qubit_base(s, n, targets, gate, q), state)
+    want = _oracle_apply(case, state, gate)
+    np.testing.assert_allclose(got, want, rtol=0, atol=PARITY_ATOL[dtype])
 
 
 @pytest.mark.parametrize("use_qubits", [False, True])

@@ -25,7 +25,8 @@ def _collapse_both(lib, ctx, state_np, dtype, n, qubits, result, normalize):
 
     from qibojit_gb300 import _lib
 
-    tdt = {"complex128": torch.complex128, "complex64": torch.complex64}[dtype]
+    tdt = {"complex128": torch.complex128, "complex64": torch.complex64, "float64": torch.float64,
+           "float32": torch.float32}[dtype]
     code = _lib.DTYPE_CODES[dtype]
     a = torch.from_numpy(state_np).to("cuda", tdt)
     b = a.clone()
@@ -42,13 +43,17 @@ def test_noalloc_collapse_matches_context_collapse():
     lib = _lib.load()
     ctx = _lib.Context(0)
     calls = [("complex128", 20, [0, 1, 2, 3], 11, True), ("complex64", 18, [5, 2, 17], 3, True),
-             ("complex128", 12, [7], 0, False)]
+             ("complex128", 12, [7], 0, False), ("float64", 16, [3, 9], 2, True), ("float32", 15, [14], 1, True)]
     for dtype, n, qubits, result, normalize in calls:
-        state = random_state(n, 100 + n, dtype)
+        if dtype.startswith("float"):
+            x = np.random.default_rng(100 + n).standard_normal(2**n)
+            state = (x / np.linalg.norm(x)).astype(dtype)
+        else:
+            state = random_state(n, 100 + n, dtype)
         want, got = _collapse_both(lib, ctx, state, dtype, n, qubits, result, normalize)
         np.testing.assert_allclose(got, want, rtol=0, atol=PARITY_ATOL[dtype])
         if normalize:
-            assert abs((np.abs(got.astype(np.complex128)) ** 2).sum() - 1) < (1e-12 if dtype == "complex128" else 1e-5)
+            assert abs((np.abs(got.astype(np.complex128)) ** 2).sum() - 1) < PARITY_ATOL[dtype]
     ctx.close()
 
 
