@@ -100,6 +100,32 @@ def _inverse_target_matrix(gate, backend) -> np.ndarray:
     return np.ascontiguousarray(full[-d:, -d:])
 
 
+def _circuit_fingerprint(circuit) -> bytes:
+    """Digest of a circuit's content: every gate's class, target and control qubits
+    and parameter values (nested gates of a FusedGate included), in queue order."""
+    import hashlib
+
+    h = hashlib.blake2b(digest_size=16)
+
+    def feed(gates):
+        for g in gates:
+            h.update(type(g).__name__.encode())
+            h.update(repr((tuple(getattr(g, "target_qubits", ())), tuple(getattr(g, "control_qubits", ())))).encode())
+            for p in getattr(g, "parameters", ()):
+                h.update(np.ascontiguousarray(p, dtype=np.complex128).tobytes())
+            coeffs = getattr(g, "coefficients", None)
+            if coeffs is not None:
+                h.update(np.asarray(coeffs, dtype=np.float64).tobytes())
+            inner = getattr(g, "gates", None)
+            if inner:
+                h.update(b"[")
+                feed(inner)
+                h.update(b"]")
+
+    feed(circuit.queue)
+    return h.digest()
+
+
 def _dtype_name(x) -> str:
     s = str(x)
     return s.replace("torch.", "").replace("numpy.", "").replace("<class '", "").replace("'>", "")
@@ -590,10 +616,12 @@ class GB300Backend(_QiboBackend):
         return state
 
     def _cached_program(self, circuit, dtype: str, upcoming_runs: int = 1, density_matrix: bool = False):
-        """The program cache of execute_circuit (one entry): a program that has run
+        """The program cache of execute_circuit (one entry), keyed by the circuit's
+        content (every gate's class, qubits and parameter values), so a different or
+        edited circuit never reuses a stale plan: a program that has run
         ``specialize_after`` times (counting the runs about to be made) is re-planned on
         the larger tile and its passes specialised."""
-        key = (id(circuit), len(circuit.queue), circuit.nqubits, dtype, bool(density_matrix))
+        key = (_circuit_fingerprint(circuit), circuit.nqubits, dtype, bool(density_matrix))
         prog = self._programs.get(key)
         if prog is None:
             prog = self.compile(circuit, dtype, density_matrix=density_matrix)

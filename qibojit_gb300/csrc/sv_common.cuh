@@ -66,6 +66,11 @@ struct Context {
   // pinned host staging for reduction results read back by the host
   void* host_pinned = nullptr;
   size_t host_pinned_bytes = 0;
+  // device status word set by kernels whose bounded waits gave up (read by sv_sync)
+  int* device_status = nullptr;
+  bool status_pending = false;
+  // dense k-target gates: SV_DENSE_AUTO, SV_DENSE_SIMT or SV_DENSE_TENSOR
+  int dense_mode = 0;
 };
 
 // error plumbing (thread-local last error string)
@@ -74,6 +79,7 @@ int check_cuda(cudaError_t e, const char* what);
 int ensure_scratch(Context* ctx, size_t bytes);
 int ensure_host_pinned(Context* ctx, size_t bytes);
 int ensure_operand(Context* ctx, size_t bytes);
+int ensure_device_status(Context* ctx);
 
 #define SV_TRY(...)                  \
   do {                               \

@@ -69,6 +69,13 @@ int ensure_operand(Context* ctx, size_t bytes) {
   return SV_OK;
 }
 
+int ensure_device_status(Context* ctx) {
+  if (ctx->device_status) return SV_OK;
+  SV_TRY(check_cuda(cudaMalloc(&ctx->device_status, sizeof(int)), "status word allocation"));
+  SV_TRY(check_cuda(cudaMemsetAsync(ctx->device_status, 0, sizeof(int), ctx->stream), "status word reset"));
+  return SV_OK;
+}
+
 }  // namespace sv
 
 extern "C" {
@@ -117,6 +124,7 @@ int sv_context_destroy(sv_context* ctx) {
   if (ctx->scratch) cudaFree(ctx->scratch);
   if (ctx->operand) cudaFree(ctx->operand);
   if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+  if (ctx->device_status) cudaFree(ctx->device_status);
   delete ctx;
   return SV_OK;
 }
@@ -127,9 +135,28 @@ int sv_context_set_stream(sv_context* ctx, void* stream) {
   return SV_OK;
 }
 
+int sv_context_set_dense_mode(sv_context* ctx, int mode) {
+  if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
+  if (mode < SV_DENSE_AUTO || mode > SV_DENSE_TENSOR) return sv::set_error(SV_ERR_ARG, "unknown dense mode %d", mode);
+  ctx->dense_mode = mode;
+  return SV_OK;
+}
+
 int sv_sync(sv_context* ctx) {
   if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
-  return sv::check_cuda(cudaStreamSynchronize(ctx->stream), "sv_sync");
+  SV_TRY(sv::check_cuda(cudaStreamSynchronize(ctx->stream), "sv_sync"));
+  if (ctx->status_pending) {
+    // kernels with bounded waits (the tensor-core gates) report a time-out here
+    ctx->status_pending = false;
+    int status = 0;
+    SV_TRY(sv::check_cuda(cudaMemcpy(&status, ctx->device_status, sizeof(int), cudaMemcpyDeviceToHost),
+                          "status word read"));
+    if (status != 0) {
+      SV_TRY(sv::check_cuda(cudaMemset(ctx->device_status, 0, sizeof(int)), "status word reset"));
+      return sv::set_error(SV_ERR_TIMEOUT, "a tensor-core gate kernel gave up waiting for its matrix operations");
+    }
+  }
+  return SV_OK;
 }
 
 }  // extern "C"

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "sv_common.cuh"
+#include "sv_dense_tc.cuh"
 
 namespace sv {
 
@@ -459,6 +460,11 @@ int sv_apply_multi_qubit(sv_context* ctx, void* state, int dtype, int nqubits, c
   BitList q;
   SV_TRY(make_bitlist(&q, nqubits, tb, ntargets, qubits, nq));
   Context* c = ctx;
+  const bool tc_ok = dense_tc_eligible(dtype, ntargets);
+  if (c->dense_mode == SV_DENSE_TENSOR && !tc_ok)
+    return set_error(SV_ERR_UNSUPPORTED, "the tensor-core kernel takes complex64 gates with 4..6 targets");
+  if (tc_ok && c->dense_mode != SV_DENSE_SIMT && (c->dense_mode == SV_DENSE_TENSOR || nqubits - q.n >= 10))
+    return dense_tc_apply(c, state, nqubits, gate, targets, ntargets, q);
   switch (dtype) {
     case SV_C128: return multi_qubit_typed<c128>(c, state, nqubits, gate, targets, ntargets, q);
     case SV_C64: return multi_qubit_typed<c64>(c, state, nqubits, gate, targets, ntargets, q);

@@ -76,3 +76,23 @@ def test_fused_program_rejects_wrong_state(backend):
         prog.run(backend.zero_state(11))
     with pytest.raises(TypeError):
         prog.run(backend.zero_state(10, dtype="complex64"))
+
+
+def test_execute_circuit_cache_follows_circuit_content(backend):
+    """Circuits built one after another (a freed circuit's id is reused by the next)
+    and a circuit edited in place each run their own gates, with the program cache
+    and its specialisation in between."""
+    x = random_state(12, 3)
+    for seed in range(5):
+        c = circuits.brickwork(12, 3, seed)
+        for _ in range(3):
+            got = backend.to_numpy(backend.execute_circuit(c, x, fuse=True))
+        want = backend.to_numpy(backend.execute_circuit(c, x, fuse=False))
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+        del c
+    c = circuits.brickwork(12, 3, 9)
+    backend.execute_circuit(c, x)
+    c.queue[0].parameters = (0.3, 0.2, 0.1)
+    got = backend.to_numpy(backend.execute_circuit(c, x, fuse=True))
+    want = backend.to_numpy(backend.execute_circuit(c, x, fuse=False))
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)

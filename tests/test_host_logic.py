@@ -159,3 +159,27 @@ def test_inverse_target_matrix(gate):
     controlled_inv = np.eye(full.shape[0], dtype=complex)
     controlled_inv[-u.shape[0]:, -u.shape[0]:] = inv
     np.testing.assert_allclose(controlled_inv, np.linalg.inv(full), atol=1e-14)
+
+
+def test_circuit_fingerprint_follows_content():
+    """execute_circuit's program cache is keyed by circuit content: equal circuits
+    share a key, and any change of a gate's parameters, qubits or class (nested
+    FusedGate components included) gives a new one."""
+    from qibojit_gb300 import circuits
+    from qibojit_gb300 import gates as G
+    from qibojit_gb300.backend import _circuit_fingerprint as fp
+
+    a, b = circuits.brickwork(8, 3, 5), circuits.brickwork(8, 3, 5)
+    assert fp(a) == fp(b)
+    b.queue[4].parameters = (0.1, 0.2, 0.3)
+    assert fp(a) != fp(b)
+    c = circuits.brickwork(8, 3, 5)
+    c.queue[-1] = G.CZ(5, 6)
+    assert fp(a) != fp(c)
+    f1, f2 = G.Circuit(3), G.Circuit(3)
+    for f, th in ((f1, 0.5), (f2, 0.6)):
+        fg = G.FusedGate(0, 1)
+        fg.append(G.RX(0, theta=th))
+        fg.append(G.CNOT(0, 1))
+        f.add(fg)
+    assert fp(f1) != fp(f2)
