@@ -72,9 +72,10 @@ int sv_context_set_stream(sv_context* ctx, void* stream);
 int sv_sync(sv_context* ctx);
 
 /* How sv_apply_multi_qubit applies dense gates: SV_DENSE_AUTO (default) runs
- * complex64 gates with 4..6 targets on the tensor cores and everything else on the
+ * complex64 gates with 5 or 6 targets on the tensor cores and everything else on the
  * CUDA cores; SV_DENSE_SIMT uses the CUDA-core kernels only; SV_DENSE_TENSOR
- * requires the tensor-core kernel (SV_ERR_UNSUPPORTED for gates it does not take).
+ * requires the tensor-core kernel, which takes complex64 gates with 4..6 targets
+ * (SV_ERR_UNSUPPORTED for others).
  * The reference has one fixed kernel per target count (gpu.py:975-1007). */
 enum sv_dense_mode { SV_DENSE_AUTO = 0, SV_DENSE_SIMT = 1, SV_DENSE_TENSOR = 2 };
 int sv_context_set_dense_mode(sv_context* ctx, int mode);
@@ -108,9 +109,9 @@ int sv_apply_two_qubit(sv_context* ctx, void* state, int dtype, int nqubits, int
  * apply_{three,four,five,multi}_qubit_gate kernels (gates.py:265-424).
  * targets: qubit indices in gate order; gate: 4^k values row-major.
  * qubits: sorted bit positions of controls and targets, or NULL / 0.
- * complex64 gates with 4..6 targets run on the tensor cores (tcgen05, TF32 operands
- * split in two, FP32 accumulation: about 2^-21 relative error per gate) unless
- * sv_context_set_dense_mode says otherwise. */
+ * complex64 gates with 5 or 6 targets run on the tensor cores (tcgen05, TF32
+ * operands split in two, FP32 accumulation: about 2^-21 relative error per gate)
+ * unless sv_context_set_dense_mode says otherwise. */
 int sv_apply_multi_qubit(sv_context* ctx, void* state, int dtype, int nqubits,
                          const void* gate, const int32_t* targets, int ntargets,
                          const int32_t* qubits, int nq);

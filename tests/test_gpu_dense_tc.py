@@ -39,6 +39,8 @@ CASES = [
     (15, [3, 1, 4, 0, 5, 2], []), (13, [6, 2, 9, 11], [0, 12]), (16, [1, 3, 5, 7, 9], [15]),
     (17, [16, 8, 4, 2, 1, 0], [10, 12]), (11, [5, 4, 3, 2, 1, 0], []), (9, [8, 7, 6, 5], [0]),
     (20, [19, 0, 10, 5, 15, 7], []), (18, [2, 3, 4, 5], [0, 1, 17]),
+    # 16 groups: half of the first warp holds groups, the other half none
+    (9, [0, 1, 2, 3], [4]), (10, [0, 1, 2, 3, 4], [6]),
 ]
 
 
@@ -123,3 +125,26 @@ def test_repeated_calls_and_sync_status(backend):
     for g in gates:
         want = ob._multi_qubit_base(want, n, targets, g, q)
     np.testing.assert_allclose(got, want, rtol=0, atol=3 * TOL)
+
+
+@pytest.mark.parametrize("targets", [[11, 10, 9, 8, 7], [3, 7, 1, 9, 0, 11]])
+def test_tensor_core_gate_on_an_8_byte_aligned_state(backend, targets):
+    """A state that starts 8 bytes past a 16-byte boundary (a view into a larger
+    buffer) takes the scalar loads and stores."""
+    import torch
+
+    n, k = 12, len(targets)
+    gate = random_unitary(2**k, 9 + k)
+    state = random_state(n, 31, "complex64")
+    buf = torch.zeros(2**n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:] = torch.from_numpy(state).to("cuda")
+    view = buf[1:]
+    assert view.data_ptr() % 16 == 8
+    backend.ctx.set_dense_mode("tensor")
+    q = O.OracleBackend.qubits_tensor(n, targets)
+    backend._multi_qubit_base(view, n, targets, gate.astype(np.complex64), q)
+    got = backend.to_numpy(view)
+    backend.synchronize()
+    want = O.OracleBackend()._multi_qubit_base(state.astype(np.complex128), n, targets, gate, q)
+    np.testing.assert_allclose(got, want, rtol=0, atol=TOL)
+    assert backend.to_numpy(buf[:1])[0] == 0
