@@ -80,6 +80,15 @@ int sv_sync(sv_context* ctx);
 enum sv_dense_mode { SV_DENSE_AUTO = 0, SV_DENSE_SIMT = 1, SV_DENSE_TENSOR = 2 };
 int sv_context_set_dense_mode(sv_context* ctx, int mode);
 
+/* Arithmetic of the complex128 one- and two-target dense gates (apply_gate,
+ * apply_z_pow, apply_two_qubit_gate, apply_fsim): SV_C128_DOUBLE_WORD (default)
+ * carries every double as a pair of floats and computes on the FP32 pipe (GB300's
+ * FP64 rate is 1/56 of FP32), about 2^-45 relative to the summed magnitudes of a
+ * gate row, a few 1e-15 absolute for amplitudes <= 1; SV_C128_FP64 uses FP64
+ * instructions.  The reference computes in FP64 (gates.py:15-254). */
+enum sv_c128_arithmetic { SV_C128_DOUBLE_WORD = 0, SV_C128_FP64 = 1 };
+int sv_context_set_c128_arithmetic(sv_context* ctx, int mode);
+
 /* ---------------------------------------------------------- state creation */
 /* |0...0>: state[0] = 1, all others 0.  Replaces ops.initial_state_vector
  * (custom_operators/ops.py:10-18) / CupyBackend.zero_state (gpu.py:584-600). */

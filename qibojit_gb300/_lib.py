@@ -25,7 +25,7 @@ TWO_KINDS = {"apply_two_qubit_gate": 0, "apply_swap": 1, "apply_fsim": 2}
 # every symbol the header declares; tests check the library exports all of them
 EXPORTS = (
     "sv_version", "sv_last_error", "sv_device_count", "sv_context_create", "sv_context_destroy",
-    "sv_context_set_stream", "sv_context_set_dense_mode", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
+    "sv_context_set_stream", "sv_context_set_dense_mode", "sv_context_set_c128_arithmetic", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
     "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_density_probabilities", "sv_axpby",
     "sv_measure_frequencies",
     "sv_collapse_state_noalloc", "sv_sample_cdf", "sv_program_create", "sv_program_run", "sv_program_stats", "sv_program_specialize", "sv_program_pass_params", "sv_pass_layout",
@@ -56,6 +56,7 @@ _SIGNATURES = {
     "sv_context_destroy": ([_vp], _int),
     "sv_context_set_stream": ([_vp, _vp], _int),
     "sv_context_set_dense_mode": ([_vp, _int], _int),
+    "sv_context_set_c128_arithmetic": ([_vp, _int], _int),
     "sv_sync": ([_vp], _int),
     "sv_zero_state": ([_vp, _vp, _int, _int], _int),
     "sv_apply_one_qubit": ([_vp, _vp, _int, _int, _int, _vp, _int, _vp, _int], _int),
@@ -167,6 +168,13 @@ class Context:
 
     def sync(self) -> None:
         check(self.lib.sv_sync(self._h), "sv_sync")
+
+    def set_c128_arithmetic(self, mode: str) -> None:
+        """'double-word' (FP32 pipe, default) or 'fp64' for the complex128 per-gate kernels."""
+        codes = {"double-word": 0, "fp64": 1}
+        if mode not in codes:
+            raise ValueError(f"complex128 arithmetic must be one of {sorted(codes)}")
+        check(self.lib.sv_context_set_c128_arithmetic(self._h, codes[mode]), "sv_context_set_c128_arithmetic")
 
     def set_dense_mode(self, mode: str) -> None:
         """'auto' (tensor cores for complex64 gates with 4..6 targets), 'simt' or 'tensor'."""

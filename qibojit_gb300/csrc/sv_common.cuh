@@ -71,6 +71,8 @@ struct Context {
   bool status_pending = false;
   // dense k-target gates: SV_DENSE_AUTO, SV_DENSE_SIMT or SV_DENSE_TENSOR
   int dense_mode = 0;
+  // complex128 per-gate arithmetic: 0 = double-word on the FP32 pipe, 1 = FP64
+  int c128_fp64 = 0;
 };
 
 // error plumbing (thread-local last error string)

@@ -142,6 +142,14 @@ int sv_context_set_dense_mode(sv_context* ctx, int mode) {
   return SV_OK;
 }
 
+int sv_context_set_c128_arithmetic(sv_context* ctx, int mode) {
+  if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
+  if (mode != SV_C128_DOUBLE_WORD && mode != SV_C128_FP64)
+    return sv::set_error(SV_ERR_ARG, "unknown complex128 arithmetic mode %d", mode);
+  ctx->c128_fp64 = mode == SV_C128_FP64;
+  return SV_OK;
+}
+
 int sv_sync(sv_context* ctx) {
   if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
   SV_TRY(sv::check_cuda(cudaStreamSynchronize(ctx->stream), "sv_sync"));

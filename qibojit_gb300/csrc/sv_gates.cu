@@ -15,10 +15,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "sv_common.cuh"
 #include "sv_dense_tc.cuh"
+#include "sv_dw.cuh"
 
 namespace sv {
 
@@ -219,6 +221,95 @@ __global__ void __launch_bounds__(kBlock) k_multi_smem(T* __restrict__ s, int64_
   }
 }
 
+// ------------------------------------------------- complex128 in double-word arithmetic
+// The same index maps and load/store pattern as k_one_qubit / k_two_qubit; every
+// amplitude is converted to a (hi, lo) float pair on load and back on store, and each
+// output is a double-word dot product (sv_dw.cuh), so the arithmetic runs on the FP32
+// pipe instead of GB300's FP64 pipe.  Operands arrive already split on the host.
+template <int KIND, bool CTRL, int ITEMS>
+__global__ void __launch_bounds__(kBlock) k_one_qubit_dw(c128* __restrict__ s, int64_t nstates, int m,
+                                                         Mat<cdw, 4> g, const __grid_constant__ BitList q) {
+  const int64_t tk = (int64_t)1 << m;
+  const int64_t base = (int64_t)blockIdx.x * (kBlock * ITEMS) + threadIdx.x;
+  int64_t i1[ITEMS];
+  double2 a[ITEMS], b[ITEMS];
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    const int64_t gi = base + (int64_t)j * kBlock;
+    i1[j] = -1;
+    if (gi < nstates) {
+      i1[j] = CTRL ? insert_ones(gi, q) - tk : insert_zero(gi, m);
+      if (KIND == SV_APPLY_GATE) a[j] = __ldcs(reinterpret_cast<const double2*>(s + i1[j]));
+      b[j] = __ldcs(reinterpret_cast<const double2*>(s + i1[j] + tk));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    if (i1[j] < 0) continue;
+    double2* p = reinterpret_cast<double2*>(s + i1[j]);
+    if constexpr (KIND == SV_APPLY_GATE) {
+      const cdw v[2] = {cdw_load(a[j]), cdw_load(b[j])};
+      __stcs(p, cdw_store(cdw_dot<2>(&g.g[0], v)));
+      __stcs(p + tk, cdw_store(cdw_dot<2>(&g.g[2], v)));
+    } else {  // SV_APPLY_Z_POW: the phase on the target-1 amplitude
+      const cdw v = cdw_load(b[j]);
+      __stcs(p + tk, cdw_store(cdw_dot<1>(&g.g[0], &v)));
+    }
+  }
+}
+
+template <int KIND, bool CTRL, int ITEMS>
+__global__ void __launch_bounds__(kBlock) k_two_qubit_dw(c128* __restrict__ s, int64_t nstates, int m1, int m2,
+                                                         int swap_targets, Mat<cdw, 16> g,
+                                                         const __grid_constant__ BitList q) {
+  const int64_t tk1 = (int64_t)1 << m1, tk2 = (int64_t)1 << m2;
+  const int64_t uk1 = swap_targets ? tk2 : tk1;
+  const int64_t uk2 = swap_targets ? tk1 : tk2;
+  const int64_t base = (int64_t)blockIdx.x * (kBlock * ITEMS) + threadIdx.x;
+  int64_t i0[ITEMS];
+  double2 v[ITEMS][4];
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    const int64_t gi = base + (int64_t)j * kBlock;
+    i0[j] = -1;
+    if (gi < nstates) {
+      i0[j] = CTRL ? insert_ones(gi, q) - tk1 - tk2 : insert_zero(insert_zero(gi, m1), m2);
+      const double2* p = reinterpret_cast<const double2*>(s + i0[j]);
+      if (KIND == SV_APPLY_TWO_QUBIT_GATE) v[j][0] = __ldcs(p);
+      v[j][1] = __ldcs(p + uk1);
+      v[j][2] = __ldcs(p + uk2);
+      v[j][3] = __ldcs(p + tk1 + tk2);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ITEMS; j++) {
+    if (i0[j] < 0) continue;
+    double2* p = reinterpret_cast<double2*>(s + i0[j]);
+    if constexpr (KIND == SV_APPLY_TWO_QUBIT_GATE) {
+      const cdw x[4] = {cdw_load(v[j][0]), cdw_load(v[j][1]), cdw_load(v[j][2]), cdw_load(v[j][3])};
+      __stcs(p, cdw_store(cdw_dot<4>(&g.g[0], x)));
+      __stcs(p + uk1, cdw_store(cdw_dot<4>(&g.g[4], x)));
+      __stcs(p + uk2, cdw_store(cdw_dot<4>(&g.g[8], x)));
+      __stcs(p + tk1 + tk2, cdw_store(cdw_dot<4>(&g.g[12], x)));
+    } else {  // fSim: 2x2 on (|01>, |10>) and a phase on |11>
+      const cdw x[2] = {cdw_load(v[j][1]), cdw_load(v[j][2])};
+      const cdw w = cdw_load(v[j][3]);
+      __stcs(p + uk1, cdw_store(cdw_dot<2>(&g.g[0], x)));
+      __stcs(p + uk2, cdw_store(cdw_dot<2>(&g.g[2], x)));
+      __stcs(p + tk1 + tk2, cdw_store(cdw_dot<1>(&g.g[4], &w)));
+    }
+  }
+}
+
+template <int N>
+static void split_operand(Mat<cdw, N>& out, const c128* in, int count) {
+  memset(&out, 0, sizeof(out));
+  for (int i = 0; i < count; i++) {
+    sv_dw_split_host(in[i].re, &out.g[i].re.h, &out.g[i].re.l);
+    sv_dw_split_host(in[i].im, &out.g[i].im.h, &out.g[i].im.l);
+  }
+}
+
 // =============================================================== host side
 static int check_state_args(const void* state, int dtype, int nqubits) {
   if (!state) return set_error(SV_ERR_ARG, "state pointer is NULL");
@@ -282,6 +373,24 @@ static int one_qubit_typed(Context* ctx, void* state, int nqubits, int kind, con
   const int m = nqubits - target - 1;
   const int ncontrols = q.n - 1;
   const int64_t nstates = (int64_t)1 << (nqubits - ncontrols - 1);
+  if constexpr (std::is_same<T, c128>::value) {
+    if (!ctx->c128_fp64 && (kind == SV_APPLY_GATE || kind == SV_APPLY_Z_POW)) {
+      Mat<cdw, 4> gd;
+      split_operand(gd, g.g, kind == SV_APPLY_GATE ? 4 : 1);
+      constexpr int ITEMS = 4;
+      const unsigned grid = grid_for(nstates, kBlock * ITEMS);
+      c128* st = (c128*)state;
+      if (kind == SV_APPLY_GATE) {
+        if (ctrl) k_one_qubit_dw<SV_APPLY_GATE, true, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m, gd, q);
+        else k_one_qubit_dw<SV_APPLY_GATE, false, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m, gd, q);
+      } else {
+        if (ctrl) k_one_qubit_dw<SV_APPLY_Z_POW, true, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m, gd, q);
+        else k_one_qubit_dw<SV_APPLY_Z_POW, false, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m, gd, q);
+      }
+      SV_LAUNCH_CHECK("one-qubit double-word kernel launch");
+      return SV_OK;
+    }
+  }
 #define SV_ONE_CASE(KIND)                                                   \
   case KIND:                                                                \
     return ctrl ? launch_one<T, KIND, true>(ctx, state, nstates, m, g, q)   \
@@ -340,6 +449,31 @@ static int two_qubit_typed(Context* ctx, void* state, int nqubits, int kind, con
   }
   const int ncontrols = q.n - 2;
   const int64_t nstates = (int64_t)1 << (nqubits - 2 - ncontrols);
+  if constexpr (std::is_same<T, c128>::value) {
+    if (!ctx->c128_fp64 && (kind == SV_APPLY_TWO_QUBIT_GATE || kind == SV_APPLY_FSIM)) {
+      Mat<cdw, 16> gd;
+      split_operand(gd, g.g, kind == SV_APPLY_FSIM ? 5 : 16);
+      constexpr int ITEMS = 2;
+      const unsigned grid = grid_for(nstates, kBlock * ITEMS);
+      c128* st = (c128*)state;
+      if (kind == SV_APPLY_TWO_QUBIT_GATE) {
+        if (ctrl)
+          k_two_qubit_dw<SV_APPLY_TWO_QUBIT_GATE, true, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m1, m2,
+                                                                                              swap, gd, q);
+        else
+          k_two_qubit_dw<SV_APPLY_TWO_QUBIT_GATE, false, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m1,
+                                                                                               m2, swap, gd, q);
+      } else {
+        if (ctrl)
+          k_two_qubit_dw<SV_APPLY_FSIM, true, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m1, m2, swap, gd, q);
+        else
+          k_two_qubit_dw<SV_APPLY_FSIM, false, ITEMS><<<grid, kBlock, 0, ctx->stream>>>(st, nstates, m1, m2, swap, gd,
+                                                                                     q);
+      }
+      SV_LAUNCH_CHECK("two-qubit double-word kernel launch");
+      return SV_OK;
+    }
+  }
 #define SV_TWO_CASE(KIND)                                                             \
   case KIND:                                                                          \
     return ctrl ? launch_two<T, KIND, true>(ctx, state, nstates, m1, m2, swap, g, q)  \
