@@ -229,11 +229,19 @@ def run_engine(args):
     circ = circuits.brickwork(n, DEPTH, SEED + rank)
     ngates = len(circ.queue)
     n_u3 = sum(1 for g in circ.queue if type(g).__name__ == "U3")
-    # the headline program: pass kernels specialised to this circuit's structure at run
-    # time (compiled once, outside the timed region)
+    # the headline program: the autotuner times the cache-blocked passes on each tile
+    # size (pass kernels specialised to this circuit's structure at run time, compiled
+    # once, outside the timed region) and the fastest is the one measured
+    from qibojit_gb300.autotune import autotune
+
     specialize = True
+    t_tune = time.perf_counter()
+    tiles = (11, 12, 13) if dtype == "complex64" else (10, 11, 12)
+    best, tune_rows = autotune(backend, circ, dtype, candidates=[("passes", t) for t in tiles], reps=1)
+    t_tune = time.perf_counter() - t_tune
+    torch.cuda.empty_cache()
     t_spec = time.perf_counter()
-    prog = backend.compile(circ, dtype, specialize=specialize)
+    prog = backend.compile(circ, dtype, tile_bits=best[1], specialize=specialize)
     t_spec = time.perf_counter() - t_spec
     st = prog.stats()
     state = backend.zero_state(n, dtype=dtype)
@@ -255,13 +263,30 @@ def run_engine(args):
         torch.distributed.barrier()
     pass_ms = (ms_step - zs_ms) / st["passes"]
 
-    # ---- end to end through the public API: pinned host -> device -> host every step
+    # ---- end to end through the public API.  Each step starts from |0...0> prepared on
+    # the device (config 2's initial state), its inputs are the gate coefficients sent
+    # with the pass launches, and its result, the final state, is read back into pinned
+    # host memory; execute_circuit_stream overlaps step k-1's read-back with step k's
+    # passes.  The variant beside it also uploads a host initial state every step.
     host_in = backend.host_buffer(n, dtype)  # pinned, on the GPU's local memory node
     host_in[0] = 1
     host_out = backend.host_buffer(n, dtype)
     for _ in range((backend.specialize_after or 0) + 1):  # plans, caches and specialises the program
         backend.execute_circuit(circ, host_in)
     torch.cuda.synchronize()
+    nbytes_state = (1 << n) * itemsize
+    link = _link_rates(torch, backend, host_out, nbytes_state)
+    e2e_steps = max(3, min(2 * args.steps, 8))
+    backend.execute_circuit_stream(circ, None, [host_out])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    backend.execute_circuit_stream(circ, None, [host_out] * e2e_steps)
+    e2e_value = ws * ngates * e2e_steps / (time.perf_counter() - t0)
+    param_bytes = backend._cached_program(circ, dtype).param_bytes()
+    # the same with the initial state uploaded from pinned host memory every step
+    t0 = time.perf_counter()
+    backend.execute_circuit_stream(circ, [host_in] * e2e_steps, [host_out] * e2e_steps)
+    e2e_roundtrip = ws * ngates * e2e_steps / (time.perf_counter() - t0)
     # one call at a time: upload, passes and read-back in sequence
     seq_steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
@@ -271,14 +296,8 @@ def run_engine(args):
         del s
     torch.cuda.synchronize()
     e2e_seq_value = ws * ngates * seq_steps / (time.perf_counter() - t0)
-    # pipelined: execute_circuit_stream overlaps step k+1's upload and step k-1's
-    # read-back with step k's passes (every step still moves the whole state both ways)
-    e2e_steps = max(3, min(2 * args.steps, 8))
     backend.execute_circuit_stream(circ, [host_in], [host_out])
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    backend.execute_circuit_stream(circ, [host_in] * e2e_steps, [host_out] * e2e_steps)
-    e2e_value = ws * ngates * e2e_steps / (time.perf_counter() - t0)
     final64 = host_out  # |psi> of the complex64 fused run, on the host
 
     # ---- variants, timed once each after one warm-up (same circuit)
@@ -324,9 +343,16 @@ def run_engine(args):
                 "zz01_c128": backend.expectation_z(s128, [0, 1], n),
             },
         }
+        variants["measurement_n30"] = _measurement_variants(torch, backend, stream, n, {"complex64": s64,
+                                                                                       "complex128": s128})
         del s128, s64
         torch.cuda.empty_cache()
+        variants["dense_gates_n30_c64"] = _dense_gate_variants(torch, backend, stream, n)
+        variants["c128_gates_n30"] = _c128_gate_variants(torch, backend, stream, n)
+        variants["fusion_k_sweep_n30_c64"] = _fusion_sweep(backend, circ)
+        torch.cuda.empty_cache()
         variants.update(_extra_workloads(torch, backend, stream, args))
+        variants["precision_n32_depth40"] = precision_report(backend, 32, 40)
 
     peak, peak_kind = _peak_hbm()
     kname = "sv_pass" if specialize else "k_fused_pass"
@@ -348,6 +374,8 @@ def run_engine(args):
                        "gates_per_step": ngates, "passes_per_step": st["passes"], "tile_bits": st["tile_bits"],
                        "pass_kernels": "specialised at run time" if specialize else "interpreting tile kernel",
                        "specialise_seconds": round(t_spec, 2) if specialize else None,
+                       "autotuned": {"pick": f"{best[0]}:{best[1]}", "seconds": round(t_tune, 2),
+                                     "candidates": tune_rows},
                        "state_bytes": nbytes, "l2": "state larger than the 129 MB L2; no flush needed",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -356,9 +384,13 @@ def run_engine(args):
                          "avg_launch_ms": pass_ms, "dense_u3_equivalent_fp32_tflops": fp32_tflops,
                          "dense_u3_equivalent_frac_of_fp32_probe_peak": fp32_tflops / FP32_PEAK_TFLOPS},
             "cpu_baseline": cb,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "steps": e2e_steps, "api": "execute_circuit_stream (pinned host states, copies overlapped)",
-                    "sequential_value": e2e_seq_value, "sequential_steps": seq_steps},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": param_bytes, "d2h_bytes_per_step": nbytes,
+                    "steps": e2e_steps,
+                    "api": "execute_circuit_stream from |0...0> on the device, final state read back into pinned "
+                           "host memory (read-back of step k-1 overlapped with step k's passes); h2d = the pass "
+                           "parameter blocks sent with the launches",
+                    "state_upload_value": e2e_roundtrip, "state_upload_h2d_bytes_per_step": nbytes,
+                    "sequential_value": e2e_seq_value, "sequential_steps": seq_steps, "link": link},
             "gpu_launches": args.steps * (st["passes"] + 1),
             "clocks": clocks.summary(),
             "variants": variants,
@@ -366,6 +398,152 @@ def run_engine(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _unitary(d, seed):
+    """Seeded Haar-random d x d unitary (QR of a complex Gaussian matrix, phases fixed)."""
+    rng = np.random.default_rng(seed)
+    q, r = np.linalg.qr(rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d)))
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def _events_ms(torch, stream, fn, reps=3):
+    """Mean device time of fn() over reps calls (CUDA events on the launching stream),
+    after one untimed call."""
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _frac(nbytes, ms):
+    peak, _ = _peak_hbm()
+    gbs = nbytes / (ms / 1000.0) / 1e9
+    return {"ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": gbs, "frac_of_hbm": gbs / peak}
+
+
+def _link_rates(torch, backend, host, nbytes):
+    """Achieved pinned host <-> device copy rates for one state (CUDA events on the
+    current stream), with the CPUs next to the GPU that the pinned pages were placed on."""
+    from qibojit_gb300.backend import _gpu_local_cpus
+
+    dev = torch.empty(host.numel(), dtype=host.dtype, device="cuda")
+    stream = torch.cuda.current_stream()
+    h2d = _events_ms(torch, stream, lambda: dev.copy_(host, non_blocking=True), reps=2)
+    d2h = _events_ms(torch, stream, lambda: host.copy_(dev, non_blocking=True), reps=2)
+    del dev
+    torch.cuda.empty_cache()
+    cpus = _gpu_local_cpus(torch.cuda.current_device())
+    return {"h2d_gbs": nbytes / (h2d / 1000.0) / 1e9, "d2h_gbs": nbytes / (d2h / 1000.0) / 1e9,
+            "pinned_on_gpu_local_cpus": sorted(cpus)[:1] + sorted(cpus)[-1:] if cpus else None}
+
+
+def _measurement_variants(torch, backend, stream, n, states):
+    """Config 2's measurement stage at n=30 on the brickwork's final states: the full
+    2^n-entry probabilities, 10^6 Metropolis shots over all qubits (the reference's
+    branch above SHOT_METROPOLIS_THRESHOLD, one chain per host thread, cpu.py:383-394,
+    ops.py:82-108) and the normalised collapse on qubits 0-3 (ops.py:63-79)."""
+    out = {}
+    for dt, s in states.items():
+        b = 16 if dt == "complex128" else 8
+        pb = 8 if dt == "complex128" else 4
+        r = {}
+        holder = {}
+
+        def probs():
+            holder["p"] = backend.calculate_probabilities(s, list(range(n)), n)
+
+        r["probabilities_all_qubits"] = _frac(b * (1 << n) + pb * (1 << n), _events_ms(torch, stream, probs))
+        p = holder["p"]
+        freqs = torch.zeros(1 << n, dtype=torch.int64, device=s.device)
+
+        def shots():
+            freqs.zero_()
+            backend.measure_frequencies_op(freqs, p, 10**6, n, 1234, backend.nthreads)
+
+        ms = _events_ms(torch, stream, shots, reps=2)
+        r["metropolis_1e6_shots"] = {"ms": ms, "chains": backend.nthreads, "shots_per_s": 1e6 / (ms / 1000.0),
+                                     "shots_counted": int(freqs.sum().item()),
+                                     "note": "one dependent random 8-byte probability read per proposal: latency-bound"}
+        del freqs, p
+        holder.clear()
+        work = torch.empty_like(s)
+
+        def collapse():
+            work.copy_(s)
+            backend.collapse_state(work, [0, 1, 2, 3], 5, n, normalize=True)
+
+        copy_ms = _events_ms(torch, stream, lambda: work.copy_(s))
+        ms = _events_ms(torch, stream, collapse) - copy_ms
+        r["collapse_qubits_0_3"] = _frac(b * (1 << n) + 2 * b * (1 << (n - 4)), ms)
+        r["collapse_qubits_0_3"]["norm2_after"] = backend.norm2(work, n)
+        del work
+        torch.cuda.empty_cache()
+        out[dt] = r
+    return out
+
+
+def _dense_gate_variants(torch, backend, stream, n):
+    """Dense k-target complex64 gates at n=30 on the tensor cores (tcgen05, TF32 split
+    in two) and on the CUDA-core kernels, targets on the highest and lowest qubits."""
+    s = backend.zero_state(n, dtype="complex64")
+    out = {}
+    for k in (4, 5, 6):
+        g = _unitary(2**k, k).astype(np.complex64)
+        for where, targets in (("high_bits", list(range(k))), ("low_bits", list(range(n - k, n)))):
+            row = {}
+            for mode in ("tensor", "simt"):
+                backend.ctx.set_dense_mode(mode)
+                ms = _events_ms(torch, stream, lambda: backend._multi_qubit_base(s, n, targets, g, None))
+                row[mode] = _frac(2 * 8 * (1 << n), ms)
+            backend.ctx.sync()
+            out[f"k{k}_{where}"] = row
+    backend.ctx.set_dense_mode("auto")
+    del s
+    torch.cuda.empty_cache()
+    return out
+
+
+def _c128_gate_variants(torch, backend, stream, n):
+    """complex128 per-gate passes at n=30: double-word arithmetic on the FP32 pipe
+    against FP64 instructions."""
+    s = backend.zero_state(n, dtype="complex128")
+    u2, u4 = _unitary(2, 1), _unitary(4, 2)
+    cases = {
+        "u3_target0": (lambda: backend._one_qubit_base(s, n, 0, "apply_gate", u2, None), 32 << n),
+        "u3_target29": (lambda: backend._one_qubit_base(s, n, n - 1, "apply_gate", u2, None), 32 << n),
+        "u1_target15": (lambda: backend._one_qubit_base(s, n, 15, "apply_z_pow", np.array(np.exp(0.3j)), None),
+                        16 << n),
+        "two_target_3_17": (lambda: backend._two_qubit_base(s, n, 3, 17, "apply_two_qubit_gate", u4, None), 32 << n),
+    }
+    out = {}
+    for name, (fn, nbytes) in cases.items():
+        row = {}
+        for mode in ("double-word", "fp64"):
+            backend.ctx.set_c128_arithmetic(mode)
+            row[mode] = _frac(nbytes, _events_ms(torch, stream, fn))
+        out[name] = row
+    backend.ctx.set_c128_arithmetic("double-word")
+    del s
+    torch.cuda.empty_cache()
+    return out
+
+
+def _fusion_sweep(backend, circ):
+    """The brickwork fused into dense blocks of k = 2..6 qubits (one HBM pass per block,
+    qibo Circuit.fuse-style; 5- and 6-qubit complex64 blocks on the tensor cores)
+    against the cache-blocked passes, each timed once by the autotuner."""
+    from qibojit_gb300.autotune import autotune
+
+    t0 = time.perf_counter()
+    best, rows = autotune(backend, circ, "complex64",
+                          candidates=[("blocks", k) for k in range(2, 7)] + [("passes", 13)], reps=1)
+    return {"pick": f"{best[0]}:{best[1]}", "table": rows, "seconds": round(time.perf_counter() - t0, 1)}
 
 
 def _extra_workloads(torch, backend, stream, args):
@@ -418,10 +596,12 @@ def _extra_workloads(torch, backend, stream, args):
     # ---- batched VQE forward, 4096 circuits
     specs = hea_batch(4096, seed=SEED)
     vq = {}
+    batches = {}
     for dt, reps in (("complex64", 3), ("complex128", 1)):
         t0 = time.perf_counter()
         bat = BatchedCircuits.from_hea(backend, specs, dt)
         create_s = time.perf_counter() - t0
+
         def timed_runs():
             bat.run()  # eager run + CUDA graph capture
             torch.cuda.synchronize()
@@ -442,17 +622,28 @@ def _extra_workloads(torch, backend, stream, args):
             ms = timed_runs()
         t0 = time.perf_counter()
         en = bat.tfim_energies(1.0)
+        st = bat.stats()
         vq[dt] = {"circuits_per_s": 4096 / (ms / 1000.0), "ms_per_batch": ms, "energy_ms":
                   1000 * (time.perf_counter() - t0), "plan_s": create_s, "specialise_s": spec_s,
-                  "interpreted_circuits_per_s": 4096 / (ms_interp / 1000.0), "stats": bat.stats()}
+                  "interpreted_circuits_per_s": 4096 / (ms_interp / 1000.0), "stats": st,
+                  # every circuit's plan passes, each one read and one write of its state
+                  "roofline": _frac(st["pass_bytes"], ms)}
         vq[dt]["energies_head"] = [float(v) for v in en[:3]]
-        if dt == "complex64":
-            e64 = en.copy()
-        else:
-            vq["max_abs_energy_diff_c64_vs_c128"] = float(np.abs(e64 - en).max())
+        batches[dt] = (bat, en)
+    (b64, e64), (b128, e128) = batches["complex64"], batches["complex128"]
+    vq["max_abs_energy_diff_c64_vs_c128"] = float(np.abs(e64 - e128).max())
+    infid = []
+    for i, nq in enumerate(b64.nqubits):
+        a, b = b128.state(i), b64.state(i)
+        ip = backend.inner_product(a, b, nq)
+        infid.append(1.0 - abs(ip) ** 2 / (backend.norm2(a, nq) * backend.norm2(b, nq)))
+    infid = np.array(infid)
+    vq["infidelity_c64_vs_c128_per_circuit"] = {"max": float(infid.max()), "median": float(np.median(infid)),
+                                                "circuits": len(infid), "normalised": True}
+    for bat, _ in batches.values():
         bat.close()
-        del bat
-        torch.cuda.empty_cache()
+    del batches, b64, b128
+    torch.cuda.empty_cache()
     # CPU baseline on a sample: the oracle's per-gate kernels on the first 8 circuits
     from qibojit_gb300.batch import hea_circuit
 
@@ -483,6 +674,34 @@ def _extra_workloads(torch, backend, stream, args):
     eng.close()
     del eng
     torch.cuda.empty_cache()
+    # complex128 on a smaller wave (its fused passes are FP64-bound), against the complex64
+    # gradients, energies and final states of the same circuits
+    w128 = 4
+    ad = {}
+    for dt in ("complex128", "complex64"):
+        e = AdjointTFIM(backend, nq, L, w128, dt, checkpoint_every=5)
+        e(prm[:w128])
+        t0 = time.perf_counter()
+        Ew, Gw = e(prm[:w128])
+        ad[dt] = (Ew, Gw, time.perf_counter() - t0, [e.state(i).clone() for i in range(w128)])
+        e.close()
+        del e
+    infid = []
+    for a, b in zip(ad["complex128"][3], ad["complex64"][3]):
+        ip = backend.inner_product(a, b, nq)
+        infid.append(1.0 - abs(ip) ** 2 / (backend.norm2(a, nq) * backend.norm2(b, nq)))
+    c128 = {"gradient_vectors_per_s": w128 / ad["complex128"][2], "wave": w128,
+            "c64_same_wave_gradient_vectors_per_s": w128 / ad["complex64"][2],
+            "max_abs_gradient_diff_c64_vs_c128": float(np.abs(ad["complex64"][1] - ad["complex128"][1]).max()),
+            "max_abs_energy_diff_c64_vs_c128": float(np.abs(ad["complex64"][0] - ad["complex128"][0]).max()),
+            "max_final_state_infidelity_c64_vs_c128": float(max(infid))}
+    del ad
+    torch.cuda.empty_cache()
+    # HBM traffic estimate: the forward plan's passes on psi, the reverse sweep's passes
+    # on psi and lambda together (its plan has one pass per forward pass), each pass one
+    # read and one write of the state; checkpoint copies left out
+    fwd_passes = backend.compile(hea_circuit(nq, L, prm[0]), "complex64").stats()["passes"]
+    adj_bytes = wave * 3 * fwd_passes * 2 * 8 * (1 << nq)
     # CPU: one forward evaluation of two layers on the oracle, scaled to a parameter-shift gradient
     c = hea_circuit(nq, 2, prm[0, :2])
     st = ob.zero_state(nq, "complex64")
@@ -500,21 +719,21 @@ def _extra_workloads(torch, backend, stream, args):
                               "s_per_wave": dt_s, "energy_head": [float(v) for v in E[:2]],
                               "cpu_parameter_shift_gradient_vectors_per_s_estimate": 1.0 / (2 * 2 * L * nq * t_eval),
                               "cpu_sample": f"2 of {L} layers forward on the oracle ({t_two:.1f} s), scaled to "
-                                            f"{2 * 2 * L * nq} shifted evaluations"}
+                                            f"{2 * 2 * L * nq} shifted evaluations",
+                              "roofline_estimate": {**_frac(adj_bytes, 1000.0 * dt_s), "forward_passes": fwd_passes},
+                              "complex128": c128}
     return out
 
 
-def run_precision(args):
+def precision_report(backend, n: int, depth: int) -> dict:
     """The precision configuration: brickwork n=32, depth 40 (1280 U3 + 620 CZ), the
     complex64 state (32 GiB) on specialised fused passes against the complex128 state
     (64 GiB) on fused passes, both on this GPU; the complex128 run is the reference
-    precision (its passes are pinned to the oracle at n <= 30 by the tests)."""
+    precision (its passes are pinned to the oracle at n <= 28 by the tests)."""
     import torch
 
-    from qibojit_gb300 import MetaBackend, circuits
+    from qibojit_gb300 import circuits
 
-    n, depth = args.precision_nqubits, 40
-    backend = MetaBackend.load("gb300")
     circ = circuits.brickwork(n, depth, SEED)
     ngates = len(circ.queue)
     stream = torch.cuda.current_stream()
@@ -538,10 +757,9 @@ def run_precision(args):
         del prog
     s64, s128 = states["complex64"], states["complex128"]
     ip = backend.inner_product(s128, s64, n)
-    line = {
-        "metric": f"precision (brickwork n={n} depth {depth})", "n_gpus": 1, "dtype": "c64 vs c128",
-        "data": "synthetic", "config": {"workload": f"brickwork n={n} depth {depth} (seed {SEED})",
-                                        "gates": ngates, "state_bytes": {"c64": 8 << n, "c128": 16 << n}},
+    rep = {
+        "workload": f"brickwork n={n} depth {depth} (seed {SEED})", "gates": ngates,
+        "state_bytes": {"c64": 8 << n, "c128": 16 << n},
         # 1 - |<psi128|psi64>|^2 (raw: includes the complex64 state's norm drift) and
         # the infidelity of the normalised states
         "infidelity_c64_vs_c128": 1.0 - abs(ip) ** 2,
@@ -553,6 +771,19 @@ def run_precision(args):
         "zz01_c128": backend.expectation_z(s128, [0, 1], n),
         "runs": out,
     }
+    del states, s64, s128
+    torch.cuda.empty_cache()
+    return rep
+
+
+def run_precision(args):
+    """``--precision``: the precision configuration on its own (one JSON line)."""
+    from qibojit_gb300 import MetaBackend
+
+    backend = MetaBackend.load("gb300")
+    rep = precision_report(backend, args.precision_nqubits, 40)
+    line = {"metric": f"precision (brickwork n={args.precision_nqubits} depth 40)", "n_gpus": 1,
+            "dtype": "c64 vs c128", "data": "synthetic", **rep}
     print(json.dumps(line), flush=True)
 
 

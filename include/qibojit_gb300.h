@@ -307,6 +307,9 @@ int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energie
 /* Device pointer and qubit count of one circuit's state. */
 int sv_batch_state(const sv_batch* b, int circuit, void** state, int* nqubits);
 int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_bytes);
+/* Algorithmic HBM bytes of one run's gate passes: for every circuit, its plan's pass
+ * count times one read and one write of its state (the |0...0> fill excluded). */
+int sv_batch_pass_bytes(const sv_batch* b, double* bytes);
 int sv_batch_destroy(sv_batch* b);
 
 /* ---------------------------------------------------------- adjoint gradients */

@@ -636,7 +636,10 @@ class GB300Backend(_QiboBackend):
 
     def execute_circuit_stream(self, circuit, host_inputs, host_outputs):
         """Runs ``circuit`` on each pinned host state of ``host_inputs`` and writes each
-        final state into the matching pinned tensor of ``host_outputs``.
+        final state into the matching pinned tensor of ``host_outputs``.  With
+        ``host_inputs=None`` every run starts from |0...0> prepared on the device (the
+        reference's default initial state, ``cpu.py:334-353``) and only the final states
+        cross the host link.
 
         States move through two device buffers on three CUDA streams: the upload of
         state k+1 and the read-back of state k-1 run while state k's passes do, so both
@@ -645,18 +648,19 @@ class GB300Backend(_QiboBackend):
         wins); an output must not be a later step's input.  Returns when every state is
         back on the host."""
         torch = _torch()
-        k_total = len(host_inputs)
+        zero_start = host_inputs is None
+        k_total = len(host_outputs) if zero_start else len(host_inputs)
         if len(host_outputs) != k_total:
             raise ValueError("need one output per input state")
         if k_total == 0:
             return host_outputs
         n = circuit.nqubits
-        dtype = _dtype_name(host_inputs[0].dtype)
+        dtype = _dtype_name((host_outputs if zero_start else host_inputs)[0].dtype)
         if n < 8 or dtype not in ("complex128", "complex64") or not circuit.queue:
-            for x, y in zip(host_inputs, host_outputs):
-                y.copy_(self.execute_circuit(circuit, x))
+            for k, y in enumerate(host_outputs):
+                y.copy_(self.execute_circuit(circuit, None if zero_start else host_inputs[k]))
             return host_outputs
-        for t in list(host_inputs) + list(host_outputs):
+        for t in ([] if zero_start else list(host_inputs)) + list(host_outputs):
             if t.is_cuda or t.numel() != (1 << n) or _dtype_name(t.dtype) != dtype:
                 raise ValueError(f"host states must hold 2^{n} {dtype} amplitudes")
         prog = self._cached_program(circuit, dtype, k_total)
@@ -677,15 +681,21 @@ class GB300Backend(_QiboBackend):
         freed = [None] * len(dev)
         self.ctx.set_stream(comp.cuda_stream)
         try:
+            dcode = _lib.DTYPE_CODES[dtype]
             for k in range(k_total):
                 b = k % len(dev)
-                with torch.cuda.stream(up):
+                if zero_start:
                     if freed[b] is not None:
-                        up.wait_event(freed[b])
-                    dev[b].copy_(host_inputs[k], non_blocking=True)
-                    loaded = torch.cuda.Event()
-                    loaded.record(up)
-                comp.wait_event(loaded)
+                        comp.wait_event(freed[b])
+                    _lib.check(self.lib.sv_zero_state(self.ctx.handle, dev[b].data_ptr(), dcode, n), "zero_state")
+                else:
+                    with torch.cuda.stream(up):
+                        if freed[b] is not None:
+                            up.wait_event(freed[b])
+                        dev[b].copy_(host_inputs[k], non_blocking=True)
+                        loaded = torch.cuda.Event()
+                        loaded.record(up)
+                    comp.wait_event(loaded)
                 prog.run(dev[b])
                 computed = torch.cuda.Event()
                 computed.record(comp)

@@ -140,7 +140,9 @@ class BatchedCircuits:
     def stats(self) -> dict:
         g, p, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
         _lib.check(self.lib.sv_batch_stats(self._h, ctypes.byref(g), ctypes.byref(p), ctypes.byref(b)))
-        return {"groups": g.value, "passes": p.value, "state_bytes": b.value}
+        pb = ctypes.c_double()
+        _lib.check(self.lib.sv_batch_pass_bytes(self._h, ctypes.byref(pb)))
+        return {"groups": g.value, "passes": p.value, "state_bytes": b.value, "pass_bytes": pb.value}
 
     def run(self) -> None:
         _lib.check(self.lib.sv_batch_run(self.ctx.handle, self._h), "sv_batch_run")

@@ -1919,6 +1919,16 @@ int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_
   return SV_OK;
 }
 
+int sv_batch_pass_bytes(const sv_batch* b, double* bytes) {
+  if (!b || !bytes) return set_error(SV_ERR_ARG, "bad batch query");
+  double total = 0.0;
+  for (auto& g : b->groups)
+    for (int c : g.circuits)
+      total += (double)g.prog->npasses * 2.0 * (double)dtype_size(b->dtype) * (double)((size_t)1 << b->nq[c]);
+  *bytes = total;
+  return SV_OK;
+}
+
 int sv_batch_destroy(sv_batch* b) {
   batch_free(b);
   return SV_OK;

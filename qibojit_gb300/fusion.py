@@ -144,6 +144,16 @@ class FusedProgram:
         return {"passes": a.value, "unfused": b.value, "fused_gates": c.value, "tile_bits": d.value,
                 "gates": self.ngates}
 
+    def param_bytes(self) -> int:
+        """Bytes of the pass parameter blocks one run sends to the device with its
+        launches (gate coefficients and the pass layout, as kernel parameters)."""
+        st = self.stats()
+        if st["passes"] == 0:
+            return 0
+        ptr, nb = ctypes.c_void_p(), ctypes.c_size_t()
+        _lib.check(self._lib.sv_program_pass_params(self._h, 0, ctypes.byref(ptr), ctypes.byref(nb)))
+        return st["passes"] * nb.value
+
     def run(self, state):
         if state.numel() != (1 << self.nqubits):
             raise ValueError("state size does not match the program")
