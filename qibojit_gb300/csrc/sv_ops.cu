@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "sv_common.cuh"
@@ -84,14 +85,34 @@ __device__ __forceinline__ int64_t kept_index(int64_t g, const Measured& m) {
 }
 
 // Pass 1 (normalize only): per-block compensated partial sums of |kept|^2.
-template <typename T>
+// CONTIG: the measured qubits are the top bits of the index, so the kept amplitudes
+// are one contiguous slice and kept_index(g) = g | value.
+template <typename T, bool CONTIG = false>
 __global__ void __launch_bounds__(kOpsBlock) k_collapse_norm_partials(
     const T* __restrict__ s, int64_t nkept, const __grid_constant__ Measured m,
     double* __restrict__ partials) {
   KSum acc;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nkept; g += stride)
-    acc.add(tnorm2(ldg_stream(s + kept_index(g, m))));
+  // 8 independent loads per thread and iteration; a complex64 state's 8 squares are
+  // summed in FP32 (to 2^-21 relative) and added to the compensated FP64 sum as one
+  // term (FP64 per amplitude would bound the pass on this GPU)
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nkept; g += 8 * stride) {
+    T v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int64_t gk = g + k * stride;
+      v[k] = gk < nkept ? ldg_stream(s + (CONTIG ? (gk | m.value) : kept_index(gk, m))) : tzero<T>();
+    }
+    if constexpr (std::is_same<T, c64>::value) {
+      float part = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 8; k++) part = fmaf(v[k].re, v[k].re, fmaf(v[k].im, v[k].im, part));
+      acc.add((double)part);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc.add(tnorm2(v[k]));
+    }
+  }
   const double r = block_sum(acc.value());
   if (threadIdx.x == 0) partials[blockIdx.x] = r;
 }
@@ -126,18 +147,24 @@ __global__ void __launch_bounds__(kOpsBlock) k_collapse_apply(T* __restrict__ s,
   using R = typename real_of<T>::type;
   const R scale = NORMALIZE ? (R)inv[1] : (R)1;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    if ((i & mask) != value) {
-      stg_stream(s + i, tzero<T>());
-    } else if (NORMALIZE) {
-      T a = ldg_stream(s + i);
-      if constexpr (is_complex<T>::value) {
-        a.re *= scale;
-        a.im *= scale;
-      } else {
-        a *= scale;
+  // four independent elements per thread and iteration keep more stores in flight
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int64_t i = i0 + k * stride;
+      if (i >= n) break;
+      if ((i & mask) != value) {
+        stg_stream(s + i, tzero<T>());
+      } else if (NORMALIZE) {
+        T a = ldg_stream(s + i);
+        if constexpr (is_complex<T>::value) {
+          a.re *= scale;
+          a.im *= scale;
+        } else {
+          a *= scale;
+        }
+        stg_stream(s + i, a);
       }
-      stg_stream(s + i, a);
     }
   }
 }
@@ -176,12 +203,25 @@ __device__ __forceinline__ double prob_at(const T* __restrict__ s, int64_t i, in
   }
 }
 
+// |s_i|^2 of a complex64 state in FP32 (one rounding more than the FP64 square
+// rounded to float; FP64 per amplitude would bound the pass on this GPU)
+__device__ __forceinline__ float norm2_f32(const c64* __restrict__ s, int64_t i) {
+  const c64 a = ldg_stream(s + i);
+  return fmaf(a.re, a.re, a.im * a.im);
+}
+// float32 output from a complex64 state: the square in FP32; otherwise FP64
+template <typename T, typename O, bool DM>
+__device__ __forceinline__ O prob_out(const T* __restrict__ s, int64_t i, int64_t dstride) {
+  if constexpr (std::is_same<T, c64>::value && std::is_same<O, float>::value && !DM) return norm2_f32(s, i);
+  else return (O)prob_at<T, DM>(s, i, dstride);
+}
+
 template <typename T, typename O, bool DM>
 __global__ void __launch_bounds__(kOpsBlock) k_probs_full(const T* __restrict__ s, int64_t n, int64_t dstride,
                                                           O* __restrict__ out) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    __stcs(out + i, (O)prob_at<T, DM>(s, i, dstride));
+    __stcs(out + i, prob_out<T, O, DM>(s, i, dstride));
 }
 
 // all qubits measured in a permuted order: out[perm(i)] = p_i
@@ -193,7 +233,7 @@ __global__ void __launch_bounds__(kOpsBlock) k_probs_perm(const T* __restrict__ 
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     int64_t o = 0;
     for (int j = 0; j < p.nq; j++) o |= ((i >> p.mpos[j]) & 1) << (p.nq - 1 - j);
-    out[o] = (O)prob_at<T, DM>(s, i, dstride);
+    out[o] = prob_out<T, O, DM>(s, i, dstride);
   }
 }
 
@@ -211,7 +251,9 @@ __global__ void __launch_bounds__(kOpsBlock) k_probs_thread_bins(const T* __rest
 }
 
 // many amplitudes per bin: block (segment, bin) sums a contiguous range of u
-template <typename T, bool DM>
+// CONTIG: every measured bit lies above the unmeasured ones, so bin o is the
+// contiguous range prob_index(o, 0) + u.
+template <typename T, bool DM, bool CONTIG = false>
 __global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restrict__ s, int64_t dstride,
                                                               int64_t per_bin, int nseg,
                                                               const __grid_constant__ ProbMap p,
@@ -221,8 +263,33 @@ __global__ void __launch_bounds__(kOpsBlock) k_probs_segments(const T* __restric
   const int64_t len = per_bin / nseg;
   const int64_t u0 = (int64_t)seg * len;
   double acc = 0.0;
-  for (int64_t u = u0 + threadIdx.x; u < u0 + len; u += blockDim.x)
-    acc += prob_at<T, DM>(s, prob_index(o, u, p), dstride);
+  const int64_t end = u0 + len;
+  const int64_t bd = blockDim.x;
+  const int64_t obase = CONTIG ? prob_index(o, 0, p) : 0;
+  if constexpr (!DM) {
+    // 8 independent loads per thread and iteration keep enough bytes in flight; a
+    // complex64 state's 8 squares are summed in FP32 and added to the FP64 sum as one
+    // term (FP64 per amplitude would bound the pass on this GPU)
+    for (int64_t u = u0 + threadIdx.x; u < end; u += 8 * bd) {
+      T v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const int64_t uk = u + k * bd;
+        v[k] = uk < end ? ldg_stream(s + (CONTIG ? obase + uk : prob_index(o, uk, p))) : tzero<T>();
+      }
+      if constexpr (std::is_same<T, c64>::value) {
+        float part = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) part = fmaf(v[k].re, v[k].re, fmaf(v[k].im, v[k].im, part));
+        acc += (double)part;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc += tnorm2(v[k]);
+      }
+    }
+  } else {
+    for (int64_t u = u0 + threadIdx.x; u < end; u += bd) acc += prob_at<T, DM>(s, prob_index(o, u, p), dstride);
+  }
   const double r = block_sum(acc);
   if (threadIdx.x == 0) partials[o * nseg + seg] = r;
 }
@@ -498,7 +565,10 @@ static int collapse_typed(Context* ctx, void* state, int nqubits, const Measured
     SV_TRY(ensure_scratch(ctx, (grid + 2) * sizeof(double)));
     double* partials = (double*)ctx->scratch;
     inv = partials + grid;
-    k_collapse_norm_partials<T><<<grid, kOpsBlock, 0, ctx->stream>>>((const T*)state, nkept, m, partials);
+    if (m.pos[0] >= nqubits - m.n)  // the measured qubits are the top bits
+      k_collapse_norm_partials<T, true><<<grid, kOpsBlock, 0, ctx->stream>>>((const T*)state, nkept, m, partials);
+    else
+      k_collapse_norm_partials<T><<<grid, kOpsBlock, 0, ctx->stream>>>((const T*)state, nkept, m, partials);
     SV_LAUNCH_CHECK("collapse norm launch");
     k_finish_inverse_norm<<<1, kOpsBlock, 0, ctx->stream>>>(partials, (int)grid, inv);
     SV_LAUNCH_CHECK("collapse norm finish launch");
@@ -540,7 +610,10 @@ static int probs_typed(Context* ctx, const void* state, int nqubits, const ProbM
   SV_TRY(ensure_scratch(ctx, (size_t)(nbins * nseg) * sizeof(double)));
   double* partials = (double*)ctx->scratch;
   dim3 grid((unsigned)nseg, (unsigned)nbins);
-  k_probs_segments<T, DM><<<grid, kOpsBlock, 0, ctx->stream>>>(s, dstride, per_bin, (int)nseg, p, partials);
+  if (!DM && p.sorted[0] >= nqubits - p.nq)  // the measured qubits are the top bits
+    k_probs_segments<T, DM, true><<<grid, kOpsBlock, 0, ctx->stream>>>(s, dstride, per_bin, (int)nseg, p, partials);
+  else
+    k_probs_segments<T, DM><<<grid, kOpsBlock, 0, ctx->stream>>>(s, dstride, per_bin, (int)nseg, p, partials);
   SV_LAUNCH_CHECK("probabilities launch");
   k_probs_finish<O><<<grid_for(nbins, kOpsBlock), kOpsBlock, 0, ctx->stream>>>(partials, nbins, (int)nseg, (O*)out);
   SV_LAUNCH_CHECK("probabilities finish launch");
