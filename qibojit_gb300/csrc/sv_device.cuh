@@ -96,9 +96,14 @@ template <> __device__ __forceinline__ void stg_stream<c64>(c64* p, c64 v) {
 }
 
 // ------------------------------------------------------------ shared-memory tile
-// element e of a tile sits at e + e/16: one padding slot per 16, so the 16-amplitude
-// columns of a phase fall into different banks
-__device__ __forceinline__ int smem_pos(int e) { return e + (e >> 4); }
+// element e of a tile sits at e + e/16 + e/256: one padding slot per 16 elements and
+// one more per 256.  The map is additive over disjoint bits (a thread's base plus a
+// register's offset), and tile bits 0-3, 4-7 and 8-11 weigh 1, 2, 4, 8 modulo the 16
+// eight-byte bank slots, so a warp whose lanes take one bit of each weight class spreads
+// its accesses over all banks (the pass generator picks such lane bits per phase).
+__host__ __device__ __forceinline__ int smem_pos(int e) { return e + (e >> 4) + (e >> 8); }
+// elements of shared memory one tile of `tsize` amplitudes occupies
+__host__ __device__ __forceinline__ int tile_stride(int tsize) { return tsize + (tsize >> 4) + (tsize >> 8); }
 
 // ------------------------------------------------------------------ cp.async
 template <int BYTES>

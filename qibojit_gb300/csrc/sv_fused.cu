@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int kt = p.kt;
   const int tsize = 1 << kt;
-  const int tstride = tsize + (tsize >> 4);
+  const int tstride = tile_stride(tsize);
   T* const buf0 = reinterpret_cast<T*>(smem_raw);  // two tiles, tstride apart
   int64_t* dep_hi = reinterpret_cast<int64_t*>(buf0 + 2 * tstride);
   const int nhi = kt - kLowBits;
@@ -714,7 +714,7 @@ static void encode_pass(const sv_program* prog, const std::vector<int>& sched, u
       int off = 0;
       for (int u = 0; u < kRB; u++)
         if ((j >> u) & 1) off |= 1 << rb[u];
-      P.soff[j] = (uint16_t)(off + (off >> 4));
+      P.soff[j] = (uint16_t)smem_pos(off);
     }
     P.op_begin = (uint16_t)nops;
     for (const Pending& pd : groups[g]) {
@@ -2007,7 +2007,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_adjoint_pass(const __grid_consta
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int kt = p.kt;
   const int tsize = 1 << kt;
-  const int tstride = tsize + (tsize >> 4);
+  const int tstride = tile_stride(tsize);
   T* const bpsi = reinterpret_cast<T*>(smem_raw);      // two psi tiles
   T* const blam = bpsi + 2 * tstride;                   // two lambda tiles
   int64_t* dep_hi = reinterpret_cast<int64_t*>(blam + 2 * tstride);
@@ -2206,7 +2206,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_adjoint_pass(const __grid_consta
 template <typename T>
 static size_t adjoint_smem(int kt, int threads) {
   const int tsize = 1 << kt;
-  return 4 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits)) +
+  return 4 * sizeof(T) * tile_stride(tsize) + sizeof(int64_t) * (1 << (kt - kLowBits)) +
          sizeof(double) * kAdjMaxGrad * (threads / 32);
 }
 

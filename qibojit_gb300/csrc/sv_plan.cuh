@@ -138,7 +138,7 @@ namespace sv {
 template <typename T>
 inline size_t pass_smem(int kt) {
   const int tsize = 1 << kt;
-  return 2 * sizeof(T) * (tsize + (tsize >> 4)) + sizeof(int64_t) * (1 << (kt - kLowBits));
+  return 2 * sizeof(T) * tile_stride(tsize) + sizeof(int64_t) * (1 << (kt - kLowBits));
 }
 
 // re-plans a program with phase folding (sv_fused.cu) unless it already has it

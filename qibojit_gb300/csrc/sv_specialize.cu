@@ -100,6 +100,51 @@ std::string deposit_expr(const char* var, const std::vector<int>& pos, bool wide
   return o.str();
 }
 
+// Shared-memory bank slot of tile element e in the padded tile layout (smem_pos), for
+// elements of `esize` bytes (a 128-byte bank row holds 128/esize slots).
+static int bank_slot(int e, int esize) { return smem_pos(e) % (128 / esize); }
+
+// Order of a phase's non-register tile bits for the thread-bit deposit: the first five
+// (a warp's lanes) are chosen so that the warp's 32 shared-memory accesses of one
+// register spread evenly over the bank slots (the ascending order can put two lanes
+// bits on the same slot weight, e.g. bits 3 and 7, doubling the wavefronts); the rest
+// stay ascending.  Loads, stores and thread-level masks of the phase all derive from
+// the same deposit, so any order is correct.
+std::vector<int> lane_order(const std::vector<int>& nonreg, int esize) {
+  if (nonreg.size() <= 5) return nonreg;
+  const int slots = 128 / esize;
+  auto cost = [&](const std::vector<int>& lanes) {
+    std::vector<int> hits(slots, 0);
+    int worst = 0;
+    for (int L = 0; L < 32; L++) {
+      int e = 0;
+      for (int i = 0; i < 5; i++)
+        if ((L >> i) & 1) e |= 1 << lanes[i];
+      worst = std::max(worst, ++hits[bank_slot(e, esize)]);
+    }
+    return worst;
+  };
+  std::vector<int> best(nonreg.begin(), nonreg.begin() + 5);
+  int best_cost = cost(best);
+  const int m = (int)nonreg.size();
+  for (int a = 0; a < m && best_cost > 32 / slots; a++)
+    for (int b = a + 1; b < m; b++)
+      for (int c = b + 1; c < m; c++)
+        for (int d = c + 1; d < m; d++)
+          for (int f = d + 1; f < m; f++) {
+            const std::vector<int> cand = {nonreg[a], nonreg[b], nonreg[c], nonreg[d], nonreg[f]};
+            const int k = cost(cand);
+            if (k < best_cost) {
+              best_cost = k;
+              best = cand;
+            }
+          }
+  std::vector<int> out = best;
+  for (int b : nonreg)
+    if (std::find(best.begin(), best.end(), b) == best.end()) out.push_back(b);
+  return out;
+}
+
 int coef_count(const FOp& f) {
   switch (f.type) {
     case FOP_D1RUN:
@@ -125,7 +170,7 @@ KernelShape shape_of(int kt) {
   k.threads = 1 << (kt - kRB);
   k.maxt = k.threads <= 256 ? 256 : 512;
   k.minb = (sizeof(T) < 16 && k.threads <= 256) ? 3 : 1;  // the interpreted pass's launch variants
-  k.smem = 2 * sizeof(T) * (size_t)((1 << kt) + (1 << (kt - kLowBits)));
+  k.smem = 2 * sizeof(T) * (size_t)tile_stride(1 << kt);
   return k;
 }
 
@@ -157,11 +202,11 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
   o << "  using T = " << ty << ";\n"
     << "  extern __shared__ __align__(16) unsigned char smem_raw[];\n"
     << "  T* const buf0 = reinterpret_cast<T*>(smem_raw);\n"
-    << "  constexpr int TSTRIDE = " << ((1 << kt) + (1 << (kt - kLowBits))) << ", SK = " << (nth + nth / 16) << ";\n"
+    << "  constexpr int TSTRIDE = " << tile_stride(1 << kt) << ";\n"
     << "  const int tid = threadIdx.x;\n"
     // tile element e = tid + k * threads: its low bits are tid's, its top four bits k's
     << "  const long long dtid = " << deposit_expr("tid", low, true) << ";\n"
-    << "  const int stid = tid + (tid >> 4);\n"
+    << "  const int stid = tid + (tid >> 4) + (tid >> 8);\n"
     << "  constexpr long long DEPK[16] = {";
   for (int k = 0; k < 16; k++) {
     long long d = 0;
@@ -169,6 +214,10 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       if ((k >> i) & 1) d |= 1ll << tpos[kt - kRB + i];
     o << d << "ll" << (k < 15 ? ", " : "};\n");
   }
+  // shared-memory position of element tid + k * threads: smem_pos is additive over the
+  // disjoint bits of tid and k * threads
+  o << "  constexpr int POSK[16] = {";
+  for (int k = 0; k < 16; k++) o << smem_pos(k * nth) << (k < 15 ? ", " : "};\n");
   if (batched) {
     const int tshift = n - kt;
     o << "  const long long nitems = " << p.ntiles << "ll * ncirc;\n"
@@ -178,7 +227,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "  auto issue_load = [&](T* buf, const T* sp, long long base) {\n"
       << "#pragma unroll\n"
       << "    for (int k = 0; k < 16; k++)\n"
-      << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, sp + (base | dtid | DEPK[k]));\n"
+      << "      sv::cp_async<sizeof(T)>(buf + stid + POSK[k], sp + (base | dtid | DEPK[k]));\n"
       << "    sv::cp_async_commit();\n"
       << "  };\n"
       << "  long long t = blockIdx.x;\n"
@@ -203,7 +252,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "  auto issue_load = [&](T* buf, long long base) {\n"
       << "#pragma unroll\n"
       << "    for (int k = 0; k < 16; k++)\n"
-      << "      sv::cp_async<sizeof(T)>(buf + stid + k * SK, state + (base | dtid | DEPK[k]));\n"
+      << "      sv::cp_async<sizeof(T)>(buf + stid + POSK[k], state + (base | dtid | DEPK[k]));\n"
       << "    sv::cp_async_commit();\n"
       << "  };\n"
       << "  long long t = blockIdx.x;\n"
@@ -226,11 +275,12 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
     std::vector<int> nonreg;
     for (int b = 0; b < kt; b++)
       if (b != P.rb[0] && b != P.rb[1] && b != P.rb[2] && b != P.rb[3]) nonreg.push_back(b);
+    nonreg = lane_order(nonreg, (int)sizeof(T));
     o << "    {  // phase " << ph << ", register bits " << (int)P.rb[0] << " " << (int)P.rb[1] << " "
       << (int)P.rb[2] << " " << (int)P.rb[3] << "\n"
       << "      const int lbase = " << deposit_expr("tid", nonreg, false) << ";\n"
       << "      (void)lbase;\n"
-      << "      T* const tp = tile + lbase + (lbase >> 4);\n"
+      << "      T* const tp = tile + lbase + (lbase >> 4) + (lbase >> 8);\n"
       << "      T v[16];\n";
     for (int j = 0; j < 16; j++) o << "      v[" << j << "] = tp[" << P.soff[j] << "];\n";
     bool uses_pn = false;
@@ -389,7 +439,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
   }
   o << "#pragma unroll\n"
     << "    for (int k = 0; k < 16; k++) sv::stg_stream(" << (batched ? "st" : "state")
-    << " + (base | dtid | DEPK[k]), tile[stid + k * SK]);\n"
+    << " + (base | dtid | DEPK[k]), tile[stid + POSK[k]]);\n"
     << "    __syncthreads();  // this buffer is refilled by the prefetch two tiles later\n"
     << "  }\n}\n";
   return o.str();
