@@ -67,6 +67,142 @@ template <> __device__ __forceinline__ double tnorm2<c64>(c64 a) {
   return (double)a.re * (double)a.re + (double)a.im * (double)a.im;
 }
 
+// ------------------------------------------------------ double-word complex128
+// GB300 runs FP64 at 1/56 of its FP32 rate.  `cw` carries a complex128 amplitude as two
+// unevaluated float pairs (hi + lo per component), 16 bytes like the complex128 it
+// stands for, and computes on the FP32 pipe: products by the error-free transformation
+// p = a*b, e = fma(a, b, -p) plus the cross terms (Dekker 1971; Joldes, Muller and
+// Popescu 2017), sums by Knuth's TwoSum, one normalisation per result: about 2^-46
+// relative per operation.  Memory keeps doubles: dw_from_double splits the 52-bit
+// mantissa into 24 + 23 bits with integer operations only (values below 2^-103 keep 24
+// bits), dw_to_double assembles both floats' bits into doubles and adds them with one
+// FP64 addition.  Range: |values| < 2^128; NaN and infinity are not carried.
+struct dw {
+  float h, l;
+};
+
+struct alignas(16) cw {
+  dw re, im;
+  cw() = default;
+  __host__ __device__ constexpr cw(dw r, dw i) : re(r), im(i) {}
+  // constants such as {1, 0}: the nearest float pair of each double
+  __host__ __device__ cw(double r, double i) : re(split(r)), im(split(i)) {}
+  static __host__ __device__ dw split(double x) {
+    dw d;
+    d.h = (float)x;
+    d.l = (float)(x - (double)d.h);
+    return d;
+  }
+};
+
+__device__ __forceinline__ dw dw_from_double(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hb = (unsigned)(b >> 32), lb = (unsigned)b;
+  const unsigned sign = hb & 0x80000000u;
+  const unsigned e = (hb >> 20) & 0x7ffu;
+  const unsigned m23 = __funnelshift_l(lb, hb, 3) & 0x7fffffu;  // mantissa bits 51..29
+  const unsigned r23 = (lb >> 6) & 0x7fffffu;                    // mantissa bits 28..6
+  dw r;
+  r.h = __uint_as_float(sign | ((e - 896u) << 23) | m23);
+  // (1 + r23 / 2^23) * 2^E' - 2^E' = r23 * 2^(E' - 23), exact (E' = e - 919 biased)
+  const unsigned eb = sign | ((e - 919u) << 23);
+  r.l = __uint_as_float(eb | r23) - __uint_as_float(eb);
+  if (e < 920u) {
+    r.l = __uint_as_float(sign);
+    if (e < 897u) r.h = __uint_as_float(sign);
+  }
+  return r;
+}
+// exact float -> double by its bits (zero and subnormal floats give a signed zero)
+__device__ __forceinline__ double double_of_float_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u, E = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  const unsigned long long bits = E == 0 ? (unsigned long long)sign << 32
+                                         : ((unsigned long long)(sign | ((E + 896u) << 20) | (m >> 3)) << 32) |
+                                               (unsigned long long)(m << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double dw_to_double(dw a) { return double_of_float_bits(a.h) + double_of_float_bits(a.l); }
+
+__device__ __forceinline__ void dw_two_sum(float a, float b, float& s, float& err) {
+  s = a + b;
+  const float bb = s - a;
+  err = (a - (s - bb)) + (b - bb);
+}
+// renormalises s + e where e is the rounding error of the operation that made s (|e|
+// at most ulp-sized against the summed products): Dekker's fast two-sum, 3 operations;
+// after cancellation, when |s| may drop below |e|, the pair still sums to s + e within
+// ulp(e), far below the magnitudes summed
+__device__ __forceinline__ dw dw_norm(float s, float e) {
+  dw r;
+  r.h = s + e;
+  r.l = e - (r.h - s);
+  return r;
+}
+// a.h * b exactly split: p + e = a*b up to the dropped a.l*b.l
+__device__ __forceinline__ float dw_prod_err(dw a, dw b, float p) {
+  return fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
+}
+__device__ __forceinline__ dw operator-(dw a) {
+  dw r;
+  r.h = -a.h;
+  r.l = -a.l;
+  return r;
+}
+__device__ __forceinline__ dw operator+(dw a, dw b) {
+  float s, e;
+  dw_two_sum(a.h, b.h, s, e);
+  return dw_norm(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ dw operator-(dw a, dw b) { return a + (-b); }
+__device__ __forceinline__ dw operator*(dw a, dw b) {
+  const float p = a.h * b.h;
+  return dw_norm(p, dw_prod_err(a, b, p));
+}
+// a1*b1 + a2*b2 (+ c), one normalisation
+__device__ __forceinline__ dw dw_dot2(dw a1, dw b1, dw a2, dw b2) {
+  const float p1 = a1.h * b1.h, p2 = a2.h * b2.h;
+  float s, t;
+  dw_two_sum(p1, p2, s, t);
+  return dw_norm(s, t + (dw_prod_err(a1, b1, p1) + dw_prod_err(a2, b2, p2)));
+}
+__device__ __forceinline__ dw dw_dot2_add(dw a1, dw b1, dw a2, dw b2, dw c) {
+  const float p1 = a1.h * b1.h, p2 = a2.h * b2.h;
+  float s, t, s2, t2;
+  dw_two_sum(p1, p2, s, t);
+  dw_two_sum(s, c.h, s2, t2);
+  return dw_norm(s2, t2 + t + c.l + (dw_prod_err(a1, b1, p1) + dw_prod_err(a2, b2, p2)));
+}
+
+// multiply-add on the real type of an amplitude: a * b + c
+__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ dw rfma(dw a, dw b, dw c) {
+  const float p = a.h * b.h;
+  float s, t;
+  dw_two_sum(p, c.h, s, t);
+  return dw_norm(s, t + (dw_prod_err(a, b, p) + c.l));
+}
+
+template <> struct real_of<cw> { using type = dw; };
+template <> struct is_complex<cw> { static constexpr bool value = true; };
+// amplitude types kept in memory as doubles and converted in registers or shared memory
+template <typename T> struct stored_as_double_pairs { static constexpr bool value = false; };
+template <> struct stored_as_double_pairs<cw> { static constexpr bool value = true; };
+template <> __device__ __forceinline__ cw tmul<cw>(cw a, cw b) {
+  return cw(dw_dot2(a.re, b.re, -a.im, b.im), dw_dot2(a.re, b.im, a.im, b.re));
+}
+template <> __device__ __forceinline__ cw tfma<cw>(cw a, cw x, cw acc) {
+  return cw(dw_dot2_add(a.re, x.re, -a.im, x.im, acc.re), dw_dot2_add(a.re, x.im, a.im, x.re, acc.im));
+}
+template <> __device__ __forceinline__ cw tzero<cw>() { return cw(dw{0.0f, 0.0f}, dw{0.0f, 0.0f}); }
+template <> __device__ __forceinline__ cw tneg<cw>(cw a) { return cw(-a.re, -a.im); }
+// a tile element written by a raw 16-byte copy of a complex128 amplitude -> cw, in place
+__device__ __forceinline__ void cw_from_stored(cw* p) {
+  const double2 d = *reinterpret_cast<const double2*>(p);
+  *p = cw(dw_from_double(d.x), dw_from_double(d.y));
+}
+
 // streaming loads/stores: each amplitude is touched once per pass
 template <typename T> __device__ __forceinline__ T ldg_stream(const T* p) { return __ldcs(p); }
 template <> __device__ __forceinline__ c128 ldg_stream<c128>(const c128* p) {
@@ -93,6 +229,10 @@ template <> __device__ __forceinline__ void stg_stream<c128>(c128* p, c128 v) {
 }
 template <> __device__ __forceinline__ void stg_stream<c64>(c64* p, c64 v) {
   __stcs(reinterpret_cast<float2*>(p), make_float2(v.re, v.im));
+}
+// a cw amplitude goes back to memory as the complex128 it stands for
+template <> __device__ __forceinline__ void stg_stream<cw>(cw* p, cw v) {
+  __stcs(reinterpret_cast<double2*>(p), make_double2(dw_to_double(v.re), dw_to_double(v.im)));
 }
 
 // ------------------------------------------------------------ shared-memory tile
@@ -179,10 +319,10 @@ __device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m
       if (!((jm >> j) & 1u)) continue;
       const int k = j | (1 << U);
       const T x = v[j], y = v[k];
-      v[j].re = fma(a, x.re, b * y.re);
-      v[j].im = fma(a, x.im, b * y.im);
-      v[k].re = fma(c, x.re, d * y.re);
-      v[k].im = fma(c, x.im, d * y.im);
+      v[j].re = rfma(a, x.re, b * y.re);
+      v[j].im = rfma(a, x.im, b * y.im);
+      v[k].re = rfma(c, x.re, d * y.re);
+      v[k].im = rfma(c, x.im, d * y.im);
     }
   }
 }
@@ -192,8 +332,8 @@ __device__ __forceinline__ void dense1r_regs(T (&v)[16], const T* __restrict__ m
 // column of row i's unit entry
 template <typename T>
 __device__ __forceinline__ T axpy_real(typename real_of<T>::type r, T x, T y) {  // r * x + y
-  if constexpr (is_complex<T>::value) return T{fma(r, x.re, y.re), fma(r, x.im, y.im)};
-  else return fma(r, x, y);
+  if constexpr (is_complex<T>::value) return T{rfma(r, x.re, y.re), rfma(r, x.im, y.im)};
+  else return rfma(r, x, y);
 }
 template <typename T, int U, int FORM>
 __device__ __forceinline__ void pivot1_regs(T (&v)[16], const T* __restrict__ m, unsigned jm) {

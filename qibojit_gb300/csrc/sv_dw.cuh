@@ -20,47 +20,15 @@
 
 #include <stdint.h>
 
+#include "sv_device.cuh"
+
 namespace sv {
 
-struct dw {
-  float h, l;
-};
-struct cdw {
-  dw re, im;
-};
+// the double-word complex type and its conversions live in sv_device.cuh (shared with
+// the pass kernels); the per-gate kernels use the accumulator below
+using cdw = cw;
 
-__device__ __forceinline__ dw dw_from_double(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const uint32_t hb = (uint32_t)(b >> 32), lb = (uint32_t)b;
-  const uint32_t sign = hb & 0x80000000u;
-  const uint32_t e = (hb >> 20) & 0x7ffu;
-  const uint32_t m23 = __funnelshift_l(lb, hb, 3) & 0x7fffffu;  // mantissa bits 51..29
-  const uint32_t r23 = (lb >> 6) & 0x7fffffu;                    // mantissa bits 28..6
-  dw r;
-  r.h = __uint_as_float(sign | ((e - 896u) << 23) | m23);
-  // (1 + r23 / 2^23) * 2^E' - 2^E' = r23 * 2^(E' - 23), exact (E' = e - 919 biased)
-  const uint32_t eb = sign | ((e - 919u) << 23);
-  r.l = __uint_as_float(eb | r23) - __uint_as_float(eb);
-  if (e < 920u) {
-    r.l = __uint_as_float(sign);
-    if (e < 897u) r.h = __uint_as_float(sign);
-  }
-  return r;
-}
-
-// exact float -> double by its bits (zero and subnormal floats give a signed zero)
-__device__ __forceinline__ double double_of_float_bits(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t sign = u & 0x80000000u, E = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-  const unsigned long long bits = E == 0 ? (unsigned long long)sign << 32
-                                         : ((unsigned long long)(sign | ((E + 896u) << 20) | (m >> 3)) << 32) |
-                                               (unsigned long long)(m << 29);
-  return __longlong_as_double((long long)bits);
-}
-
-__device__ __forceinline__ double dw_to_double(dw a) { return double_of_float_bits(a.h) + double_of_float_bits(a.l); }
-
-__device__ __forceinline__ cdw cdw_load(const double2& v) { return {dw_from_double(v.x), dw_from_double(v.y)}; }
+__device__ __forceinline__ cdw cdw_load(const double2& v) { return cdw(dw_from_double(v.x), dw_from_double(v.y)); }
 __device__ __forceinline__ double2 cdw_store(const cdw& a) { return make_double2(dw_to_double(a.re), dw_to_double(a.im)); }
 
 // (sum, error) accumulator of products: value = s + e, normalised by dwacc_result
@@ -95,7 +63,7 @@ __device__ __forceinline__ dw dwacc_result(dwacc acc) {
   two_sum(acc.s, acc.e, r.h, r.l);
   return r;
 }
-__device__ __forceinline__ dw dw_neg(dw a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dw dw_neg(dw a) { return -a; }
 
 // complex sum_k m_k * v_k over N terms
 template <int N>
@@ -110,7 +78,7 @@ __device__ __forceinline__ cdw cdw_dot(const cdw* m, const cdw* v) {
     dw_fma(im, m[k].re, v[k].im);
     dw_fma(im, m[k].im, v[k].re);
   }
-  return {dwacc_result(re), dwacc_result(im)};
+  return cdw(dwacc_result(re), dwacc_result(im));
 }
 
 }  // namespace sv

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <complex>
+#include <type_traits>
 #include <vector>
 
 #include "sv_plan.cuh"
@@ -187,6 +188,12 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
       cp_async_wait<0>();
     }
     __syncthreads();
+    if constexpr (stored_as_double_pairs<T>::value) {
+      // the tile arrived as complex128 bytes: convert it to float pairs in place, once
+      // per pass (the final stores convert back)
+      for (int e = threadIdx.x; e < tsize; e += nthreads) cw_from_stored(tile + smem_pos(e));
+      __syncthreads();
+    }
     for (int ph = 0; ph < p.nphases; ph++) {
       const Phase& P = p.phases[ph];
       const int r0 = P.rb[0], r1 = P.rb[1], r2 = P.rb[2], r3 = P.rb[3];
@@ -1095,6 +1102,9 @@ static int launch_pass(Context* ctx, const PassParams<T>& p, void* state, int th
 
 template <typename T>
 static int run_program(Context* ctx, const sv_program* prog, void* state) {
+  constexpr bool kDW = stored_as_double_pairs<T>::value;
+  const std::vector<unsigned char>& blocks = kDW ? prog->passes_dw : prog->passes;
+  const bool spec = prog->spec && specialized_is_dw(prog->spec) == kDW;
   const int n = prog->nqubits, kt = prog->kt;
   const size_t smem = pass_smem<T>(kt);
   const int threads = 1 << (kt - kRB);
@@ -1105,8 +1115,8 @@ static int run_program(Context* ctx, const sv_program* prog, void* state) {
   for (const Segment& s : prog->segments) {
     if (s.fused) {
       const PassParams<T>& p =
-          *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
-      if (prog->spec) SV_TRY(specialized_launch(ctx, prog, s.pass, state));
+          *reinterpret_cast<const PassParams<T>*>(blocks.data() + (size_t)s.pass * prog->pass_bytes);
+      if (spec) SV_TRY(specialized_launch(ctx, prog, s.pass, state));
       else SV_TRY(launch_pass<T>(ctx, p, state, threads, smem, ntiles, ctx->stream));
     } else {
       const HostOp& h = prog->ops[s.host_op];
@@ -1118,13 +1128,14 @@ static int run_program(Context* ctx, const sv_program* prog, void* state) {
       for (int i = 0; i < h.nc; i++) qubits.push_back(h.cpos[i]);
       std::sort(qubits.begin(), qubits.end());
       const size_t d = (size_t)1 << h.nt;
-      std::vector<T> dense(d * d);
+      using E = typename std::conditional<kDW, c128, T>::type;  // the operand in the state's dtype
+      std::vector<E> dense(d * d);
       if (h.kind == SV_OP_DIAG) {  // a diagonal on more than 3 bits: apply as a dense matrix
         const double zero[2] = {0.0, 0.0};
-        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<T>(zero);
-        for (size_t i = 0; i < d; i++) dense[i * d + i] = to_elem<T>(&h.m[2 * i]);
+        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<E>(zero);
+        for (size_t i = 0; i < d; i++) dense[i * d + i] = to_elem<E>(&h.m[2 * i]);
       } else {
-        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<T>(&h.m[2 * i]);
+        for (size_t i = 0; i < d * d; i++) dense[i] = to_elem<E>(&h.m[2 * i]);
       }
       SV_TRY(sv_apply_multi_qubit(static_cast<sv_context*>(ctx), state, prog->dtype, n, dense.data(), targets.data(),
                                   h.nt, qubits.data(), (int)qubits.size()));
@@ -1384,6 +1395,20 @@ static int check_tile_bits(int dtype, int nqubits, int tile_bits, int* kt_out) {
   return SV_OK;
 }
 
+// complex128 programs also keep their pass blocks with every coefficient split into the
+// nearest float pair (round to nearest, then the remainder), for the double-word kernels
+static void make_dw_blocks(sv_program* prog) {
+  static_assert(sizeof(PassParams<cw>) == sizeof(PassParams<c128>), "double-word blocks mirror complex128 ones");
+  static_assert(offsetof(PassParams<cw>, coef) == offsetof(PassParams<c128>, coef), "same coefficient offset");
+  prog->passes_dw = prog->passes;
+  constexpr size_t ncoef = sizeof(PassParams<c128>::coef) / sizeof(c128);
+  for (int i = 0; i < prog->npasses; i++) {
+    const auto* src = reinterpret_cast<const PassParams<c128>*>(prog->passes.data() + (size_t)i * prog->pass_bytes);
+    auto* dst = reinterpret_cast<PassParams<cw>*>(prog->passes_dw.data() + (size_t)i * prog->pass_bytes);
+    for (size_t k = 0; k < ncoef; k++) dst->coef[k] = cw(src->coef[k].re, src->coef[k].im);
+  }
+}
+
 static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_program** out,
                 bool fold_diagonals = false, bool pack = true) {
   if (kt > nqubits || kt < kLowBits + kRB) return set_error(SV_ERR_ARG, "tile of %d bits for %d qubits", kt, nqubits);
@@ -1399,6 +1424,7 @@ static int plan(int dtype, int nqubits, int kt, std::vector<HostOp>&& ops, sv_pr
     delete prog;
     return rc;
   }
+  if (dtype == SV_C128) make_dw_blocks(prog);
   *out = prog;
   return SV_OK;
 }
@@ -1413,7 +1439,10 @@ int refold_program(sv_program* prog) {
   prog->pass_coef_off.clear();
   prog->coef_total = 0;
   prog->npasses = prog->nunfused = prog->nfused_gates = prog->nphases = 0;
-  return prog->dtype == SV_C128 ? build_program<c128>(prog) : build_program<c64>(prog);
+  if (prog->dtype != SV_C128) return build_program<c64>(prog);
+  SV_TRY(build_program<c128>(prog));
+  make_dw_blocks(prog);
+  return SV_OK;
 }
 
 }  // namespace sv
@@ -1445,7 +1474,9 @@ int sv_program_create(sv_context* ctx, int dtype, int nqubits, const sv_gate_op*
 int sv_program_run(sv_context* ctx, const sv_program* prog, void* state) {
   if (!ctx || !prog || !state) return set_error(SV_ERR_ARG, "null context, program or state");
   if (((uintptr_t)state) % 16) return set_error(SV_ERR_ARG, "state must be 16-byte aligned");
-  return prog->dtype == SV_C128 ? run_program<c128>(ctx, prog, state) : run_program<c64>(ctx, prog, state);
+  if (prog->dtype == SV_C128)  // double-word arithmetic unless the context asks for FP64
+    return ctx->c128_fp64 ? run_program<c128>(ctx, prog, state) : run_program<cw>(ctx, prog, state);
+  return run_program<c64>(ctx, prog, state);
 }
 
 int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* nfused_gates, int* tile_bits) {

@@ -112,6 +112,9 @@ struct sv_program {
   std::vector<sv::Segment> segments;
   std::vector<unsigned char> passes;  // PassParams<T> blocks, back to back
   size_t pass_bytes = 0;
+  // complex128 programs: the same blocks with every coefficient split into float pairs
+  // (PassParams<cw>, read by the double-word pass kernels)
+  std::vector<unsigned char> passes_dw;
   // coefficient sources of all passes, back to back: (op index, entry) per slot
   std::vector<int32_t> coef_src;
   std::vector<size_t> pass_coef_off;
@@ -145,6 +148,8 @@ inline size_t pass_smem(int kt) {
 int refold_program(sv_program* prog);
 // launches pass `pass` of a specialised program on the context stream
 int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state);
+// whether a specialised program's kernels compute in double-word arithmetic (cw)
+bool specialized_is_dw(const Specialized* s);
 // compiles the batched pass kernels of an (unfolded) program into prog->bspec
 int specialize_batched(Context* ctx, sv_program* prog);
 // launches batched pass `pass` over ncirc circuits: state pointer table, coefficient blocks

@@ -22,6 +22,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <condition_variable>
 #include <memory>
 #include <mutex>
@@ -181,7 +182,12 @@ KernelShape shape_of(int kt) {
 template <typename T>
 std::string pass_source(const PassParams<T>& p, const char* name, bool batched = false) {
   std::ostringstream o;
-  const char* ty = sizeof(T) == 16 ? "sv::c128" : "sv::c64";
+  const char* ty = stored_as_double_pairs<T>::value ? "sv::cw" : (sizeof(T) == 16 ? "sv::c128" : "sv::c64");
+  // double-word passes convert the tile to float pairs in place once it has arrived
+  const char* conv = stored_as_double_pairs<T>::value
+                         ? "#pragma unroll\n    for (int k = 0; k < 16; k++) sv::cw_from_stored(tile + stid + POSK[k]);\n"
+                           "    __syncthreads();\n"
+                         : "";
   const int kt = p.kt, n = p.n;
   const KernelShape ks = shape_of<T>(kt);
   const int nth = ks.threads;
@@ -245,7 +251,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "    } else {\n"
       << "      sv::cp_async_wait<0>();\n"
       << "    }\n"
-      << "    __syncthreads();\n";
+      << "    __syncthreads();\n" << conv;
   } else {
     o << "  const long long nitems = " << p.ntiles << "ll;\n"
       << "  auto origin = [&](long long t) -> long long { return " << deposit_expr("t", outer, true) << "; };\n"
@@ -268,7 +274,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "    } else {\n"
       << "      sv::cp_async_wait<0>();\n"
       << "    }\n"
-      << "    __syncthreads();\n";
+      << "    __syncthreads();\n" << conv;
   }
   for (int ph = 0; ph < p.nphases; ph++) {
     const Phase& P = p.phases[ph];
@@ -580,7 +586,10 @@ struct PassKernel {
 
 struct Specialized {
   std::vector<PassKernel> passes;  // indexed like the program's pass blocks
+  bool dw = false;                 // compiled for double-word complex128 (cw)
 };
+
+bool specialized_is_dw(const Specialized* s) { return s && s->dw; }
 
 void specialized_free(Specialized* s) { delete s; }
 
@@ -674,7 +683,12 @@ static int specialize_typed(Context* ctx, sv_program* prog) {
   // specialised passes run the phase-folded plan fastest (no op decoding to pay for)
   SV_TRY(refold_program(prog));
   std::unique_ptr<Specialized> s;
-  SV_TRY(build_kernels<T>(ctx, prog, false, &s));
+  if (std::is_same<T, c128>::value && !ctx->c128_fp64) {  // complex128 in double-word arithmetic
+    SV_TRY(build_kernels<cw>(ctx, prog, false, &s));
+    s->dw = true;
+  } else {
+    SV_TRY(build_kernels<T>(ctx, prog, false, &s));
+  }
   if (prog->spec) specialized_free(prog->spec);
   prog->spec = s.release();
   return SV_OK;
@@ -709,9 +723,11 @@ int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, c
 
 int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state) {
   const PassKernel& pk = prog->spec->passes[pass];
-  const unsigned char* block = prog->passes.data() + (size_t)pass * prog->pass_bytes;
-  const void* coef = prog->dtype == SV_C128 ? (const void*)reinterpret_cast<const PassParams<c128>*>(block)->coef
-                                            : (const void*)reinterpret_cast<const PassParams<c64>*>(block)->coef;
+  const bool dw = prog->spec->dw;
+  const unsigned char* block = (dw ? prog->passes_dw : prog->passes).data() + (size_t)pass * prog->pass_bytes;
+  const void* coef = dw ? (const void*)reinterpret_cast<const PassParams<cw>*>(block)->coef
+                        : prog->dtype == SV_C128 ? (const void*)reinterpret_cast<const PassParams<c128>*>(block)->coef
+                                                 : (const void*)reinterpret_cast<const PassParams<c64>*>(block)->coef;
   const int64_t ntiles = (int64_t)1 << (prog->nqubits - prog->kt);
   int64_t grid = (int64_t)pk.per_sm * ctx->num_sms;
   if (grid > ntiles) grid = ntiles;

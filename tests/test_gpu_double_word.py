@@ -117,3 +117,23 @@ def test_double_word_circuit_depth(backend):
 def test_double_word_mode_is_rejected_when_unknown(backend):
     with pytest.raises(ValueError):
         backend.ctx.set_c128_arithmetic("fp32")
+
+
+@pytest.mark.parametrize("specialize", [False, True])
+def test_fused_program_double_word_vs_fp64(backend, specialize):
+    """The fused complex128 passes in double-word arithmetic (tile converted to float
+    pairs in shared memory once per pass) against the same program in FP64, on a
+    random circuit of every fusable family and on the brickwork."""
+    from qibojit_gb300 import circuits
+    from tests.circuits_random import random_circuit
+
+    for circ in (random_circuit(14, 160, 3), circuits.brickwork(16, 12, 4)):
+        n = circ.nqubits
+        x = random_state(n, 12)
+        outs = {}
+        for mode in ("double-word", "fp64"):
+            backend.ctx.set_c128_arithmetic(mode)
+            prog = backend.compile(circ, "complex128", specialize=specialize)
+            outs[mode] = backend.to_numpy(prog.run(backend.cast(x, dtype="complex128", copy=True)))
+        backend.ctx.set_c128_arithmetic("double-word")
+        np.testing.assert_allclose(outs["double-word"], outs["fp64"], rtol=0, atol=PARITY_ATOL["complex128"])
