@@ -1545,6 +1545,7 @@ struct BatchGroup {
   sv_program* prog = nullptr;
   std::vector<int> circuits;
   void* d_coef = nullptr;      // ncirc x coef_total elements
+  void* d_coef_dw = nullptr;   // complex128 batches: the same, split into float pairs (cw)
   void* d_states = nullptr;    // ncirc device pointers
 };
 
@@ -1552,6 +1553,7 @@ struct BatchGroup {
 
 struct sv_batch {
   int dtype = 0, ncirc = 0, kt = 0;
+  bool dw = false;                     // complex128 passes in double-word arithmetic
   std::vector<int> nq;
   std::vector<size_t> off;             // element offset of each circuit's state
   size_t total = 0;                    // elements
@@ -1679,6 +1681,15 @@ static int batch_build(sv_batch* b) {
     if (ct) {
       SV_TRY(check_cuda(cudaMalloc(&g.d_coef, nc * ct * sizeof(T)), "batch coefficients"));
       SV_TRY(check_cuda(cudaMemcpy(g.d_coef, coef.data(), nc * ct * sizeof(T), cudaMemcpyHostToDevice), "coef upload"));
+      if constexpr (std::is_same<T, c128>::value) {
+        if (b->dw) {
+          std::vector<cw> split(nc * ct);
+          for (size_t k = 0; k < nc * ct; k++) split[k] = cw(coef[k].re, coef[k].im);
+          SV_TRY(check_cuda(cudaMalloc(&g.d_coef_dw, nc * ct * sizeof(cw)), "batch coefficients"));
+          SV_TRY(check_cuda(cudaMemcpy(g.d_coef_dw, split.data(), nc * ct * sizeof(cw), cudaMemcpyHostToDevice),
+                            "coef upload"));
+        }
+      }
     }
     SV_TRY(check_cuda(cudaMalloc(&g.d_states, nc * sizeof(T*)), "batch pointers"));
     SV_TRY(check_cuda(cudaMemcpy(g.d_states, ptrs.data(), nc * sizeof(T*), cudaMemcpyHostToDevice), "pointer upload"));
@@ -1715,9 +1726,24 @@ static int batch_launches(Context* ctx, sv_batch* b) {
     args.ncirc = (int32_t)g.circuits.size();
     for (const Segment& s : prog->segments) {
       if (prog->bspec) {
-        SV_TRY(specialized_launch_batched(ctx, prog, s.pass, st, g.d_states, g.d_coef, (int64_t)prog->coef_total,
+        SV_TRY(specialized_launch_batched(ctx, prog, s.pass, st, g.d_states, b->dw ? g.d_coef_dw : g.d_coef,
+                                          (int64_t)prog->coef_total,
                                           args.ncirc));
         continue;
+      }
+      if constexpr (std::is_same<T, c128>::value) {
+        if (b->dw) {  // double-word kernels on the pre-split blocks and coefficients
+          BatchArgs<cw> a;
+          memset(&a, 0, sizeof(a));
+          a.states = (cw* const*)g.d_states;
+          a.coef = (const cw*)g.d_coef_dw;
+          a.coef_stride = args.coef_stride;
+          a.ncirc = args.ncirc;
+          const PassParams<cw>& p =
+              *reinterpret_cast<const PassParams<cw>*>(prog->passes_dw.data() + (size_t)s.pass * prog->pass_bytes);
+          SV_TRY(launch_pass<cw, true>(ctx, p, nullptr, threads, smem, p.ntiles * a.ncirc, st, a));
+          continue;
+        }
       }
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)s.pass * prog->pass_bytes);
@@ -1737,6 +1763,7 @@ static void batch_free(sv_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (auto& g : b->groups) {
     if (g.d_coef) cudaFree(g.d_coef);
+    if (g.d_coef_dw) cudaFree(g.d_coef_dw);
     if (g.d_states) cudaFree(g.d_states);
     sv_program_destroy(g.prog);
   }
@@ -1767,6 +1794,9 @@ int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubit
   SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
   sv_batch* b = new sv_batch();
   b->dtype = dtype;
+  // complex128 batches compute in double-word arithmetic unless the context asks for
+  // FP64 when the batch is created (fixed for its life: its runs replay one graph)
+  b->dw = dtype == SV_C128 && !ctx->c128_fp64;
   b->ncirc = ncirc;
   const size_t es = dtype_size(dtype);
   // parse every circuit through the program front end (validation included)
@@ -1868,7 +1898,7 @@ int sv_batch_specialize(sv_context* ctx, sv_batch* b) {
   if (!ctx || !b) return set_error(SV_ERR_ARG, "null context or batch");
   SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
   SV_TRY(check_cuda(cudaDeviceSynchronize(), "batch specialise sync"));
-  for (auto& g : b->groups) SV_TRY(specialize_batched(ctx, g.prog));
+  for (auto& g : b->groups) SV_TRY(specialize_batched(ctx, g.prog, b->dw));
   // the recorded graph holds the interpreting launches: record again on the next run
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);

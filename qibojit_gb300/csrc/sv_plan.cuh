@@ -150,8 +150,9 @@ int refold_program(sv_program* prog);
 int specialized_launch(Context* ctx, const sv_program* prog, int pass, void* state);
 // whether a specialised program's kernels compute in double-word arithmetic (cw)
 bool specialized_is_dw(const Specialized* s);
-// compiles the batched pass kernels of an (unfolded) program into prog->bspec
-int specialize_batched(Context* ctx, sv_program* prog);
+// compiles the batched pass kernels of an (unfolded) program into prog->bspec; dw:
+// complex128 kernels in double-word arithmetic (coefficients passed as cw)
+int specialize_batched(Context* ctx, sv_program* prog, bool dw);
 // launches batched pass `pass` over ncirc circuits: state pointer table, coefficient blocks
 int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, cudaStream_t stream, void* states,
                                const void* coef, int64_t coef_stride, int ncirc);

@@ -694,14 +694,19 @@ static int specialize_typed(Context* ctx, sv_program* prog) {
   return SV_OK;
 }
 
-int specialize_batched(Context* ctx, sv_program* prog) {
+int specialize_batched(Context* ctx, sv_program* prog, bool dw) {
   if (!nvrtc().ok)
     return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
   // batched programs keep the unfolded plan: every circuit's coefficients are its own
   // gates' entries, gathered through the plan's coefficient-source map
   if (prog->fold_diagonals) return set_error(SV_ERR_ARG, "batched passes need an unfolded program");
   std::unique_ptr<Specialized> s;
-  SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, true, &s) : build_kernels<c64>(ctx, prog, true, &s));
+  if (prog->dtype == SV_C128 && dw) {
+    SV_TRY(build_kernels<cw>(ctx, prog, true, &s));
+    s->dw = true;
+  } else {
+    SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, true, &s) : build_kernels<c64>(ctx, prog, true, &s));
+  }
   if (prog->bspec) specialized_free(prog->bspec);
   prog->bspec = s.release();
   return SV_OK;

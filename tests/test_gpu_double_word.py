@@ -137,3 +137,28 @@ def test_fused_program_double_word_vs_fp64(backend, specialize):
             outs[mode] = backend.to_numpy(prog.run(backend.cast(x, dtype="complex128", copy=True)))
         backend.ctx.set_c128_arithmetic("double-word")
         np.testing.assert_allclose(outs["double-word"], outs["fp64"], rtol=0, atol=PARITY_ATOL["complex128"])
+
+
+@pytest.mark.parametrize("specialize", [False, True])
+def test_batched_circuits_double_word_vs_fp64(backend, specialize):
+    """Batched complex128 circuits (the arithmetic is fixed when the batch is created)
+    in double-word arithmetic against the same batch in FP64: every state and every
+    TFIM energy."""
+    from qibojit_gb300.batch import BatchedCircuits, hea_batch, hea_circuit
+
+    specs = hea_batch(24, seed=29, nmin=8, nmax=14, lmin=2, lmax=5)
+    circs = [hea_circuit(n, L, p) for n, L, p in specs]
+    states, energies = {}, {}
+    for mode in ("double-word", "fp64"):
+        backend.ctx.set_c128_arithmetic(mode)
+        batch = BatchedCircuits(backend, circs, "complex128")
+        backend.ctx.set_c128_arithmetic("double-word")
+        if specialize:
+            batch.specialize()
+        batch.run()
+        states[mode] = [backend.to_numpy(batch.state(i)) for i in range(len(circs))]
+        energies[mode] = np.asarray(batch.tfim_energies(1.0))
+        del batch
+    for a, b in zip(states["double-word"], states["fp64"]):
+        np.testing.assert_allclose(a, b, rtol=0, atol=PARITY_ATOL["complex128"])
+    np.testing.assert_allclose(energies["double-word"], energies["fp64"], rtol=0, atol=1e-11)
