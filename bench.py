@@ -669,7 +669,7 @@ def _extra_workloads(torch, backend, stream, args):
     # ---- adjoint gradients: one wave of 64 circuits, n=26, 20 layers, complex64
     nq, L, wave = 26, 20, 64
     prm = np.random.default_rng(SEED).uniform(0, 2 * np.pi, size=(wave, L, nq, 2))
-    eng = AdjointTFIM(backend, nq, L, wave, "complex64", checkpoint_every=5)
+    eng = AdjointTFIM(backend, nq, L, wave, "complex64", checkpoint_every=5, specialize=True)
     eng(prm)  # plans and allocates
     t0 = time.perf_counter()
     E, G = eng(prm)
@@ -682,7 +682,7 @@ def _extra_workloads(torch, backend, stream, args):
     w128 = 4
     ad = {}
     for dt in ("complex128", "complex64"):
-        e = AdjointTFIM(backend, nq, L, w128, dt, checkpoint_every=5)
+        e = AdjointTFIM(backend, nq, L, w128, dt, checkpoint_every=5, specialize=True)
         e(prm[:w128])
         t0 = time.perf_counter()
         Ew, Gw = e(prm[:w128])

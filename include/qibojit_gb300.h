@@ -331,6 +331,12 @@ int sv_adjoint_update(sv_context* ctx, sv_adjoint* A, const sv_gate_op* const* o
 /* Forward + reverse sweep: energies (host, ncirc) and gradients (host, ncirc x nparams,
  * row-major); either may be NULL.  Synchronises. */
 int sv_adjoint_run(sv_context* ctx, sv_adjoint* A, double h, double* energies, double* grads);
+/* Compiles the forward passes (as sv_batch_specialize) and the reverse-sweep passes
+ * (psi and lambda tiles, every gradient marker as literals) of every segment with the
+ * structure fixed in the source; later runs launch them, and sv_adjoint_update keeps
+ * them (coefficients stay in device arrays).  SV_ERR_UNSUPPORTED when libnvrtc is
+ * absent. */
+int sv_adjoint_specialize(sv_context* ctx, sv_adjoint* A);
 /* Device pointer of a circuit's final forward state (valid after a run, until the next). */
 int sv_adjoint_state(const sv_adjoint* A, int circuit, void** psi);
 int sv_adjoint_destroy(sv_adjoint* A);

@@ -36,7 +36,7 @@ def _hea_structure(n: int, layers: int):
 
 class AdjointTFIM:
     def __init__(self, backend, nqubits: int, layers: int, ncirc: int, dtype: str = "complex64", h: float = 1.0,
-                 checkpoint_every: int = 5, tile_bits: int = 0):
+                 checkpoint_every: int = 5, tile_bits: int = 0, specialize: bool = False):
         self.backend = backend
         self.ctx = backend.ctx
         self.lib = backend.lib
@@ -51,6 +51,10 @@ class AdjointTFIM:
                                                                             // checkpoint_every + 1)]
         ends[-1] = self.nops
         self.segment_ends = np.array(ends, dtype=np.int32)
+        self.tile_bits = int(tile_bits)
+        # compile every forward and reverse-sweep pass with the structure as literals
+        # (NVRTC) when the engine is created; the interpreting kernels otherwise
+        self.specialize = bool(specialize)
         self._h = None
 
     # op arrays for all circuits (vectorised matrices, then one struct per op)
@@ -96,9 +100,11 @@ class AdjointTFIM:
             _lib.check(self.lib.sv_adjoint_create(self.ctx.handle, _lib.DTYPE_CODES[self.dtype], self.ncirc, self.n,
                                                   arrays, self.nops, self.gens.ctypes.data,
                                                   self.params_idx.ctypes.data, self.nparams,
-                                                  self.segment_ends.ctypes.data, len(self.segment_ends), 0,
-                                                  ctypes.byref(h)), "sv_adjoint_create")
+                                                  self.segment_ends.ctypes.data, len(self.segment_ends),
+                                                  self.tile_bits, ctypes.byref(h)), "sv_adjoint_create")
             self._h = h
+            if self.specialize:
+                _lib.check(self.lib.sv_adjoint_specialize(self.ctx.handle, self._h), "sv_adjoint_specialize")
         else:
             _lib.check(self.lib.sv_adjoint_update(self.ctx.handle, self._h, arrays, self.nops, self.gens.ctypes.data,
                                                   self.params_idx.ctypes.data), "sv_adjoint_update")

@@ -375,4 +375,44 @@ __device__ __forceinline__ void apply_negations(T (&v)[16], unsigned nm) {
     if ((nm >> j) & 1u) v[j] = tneg(v[j]);
 }
 
+// adjoint gradients: products in the state's own precision (FP32 for complex64, FP64
+// for complex128); the callers sum warps and blocks in FP64
+template <typename T>
+__device__ __forceinline__ typename real_of<T>::type im_cdot(T a, T b) {  // Im(conj(a) b)
+  if constexpr (is_complex<T>::value) return a.re * b.im - a.im * b.re;
+  else return 0;
+}
+template <typename T>
+__device__ __forceinline__ typename real_of<T>::type re_cdot(T a, T b) {  // Re(conj(a) b)
+  if constexpr (is_complex<T>::value) return a.re * b.re + a.im * b.im;
+  else return a * b;
+}
+// Im <w| G |v> over the register pairs of bit U for the generator G = X (GEN 1) or
+// Y (GEN 2): the derivative of exp(-i t G / 2) is -i G / 2 times it
+template <typename T, int U, int GEN>
+__device__ __forceinline__ typename real_of<T>::type grad_pairs(const T (&v)[16], const T (&w)[16]) {
+  typename real_of<T>::type acc = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    if (j & (1 << U)) continue;
+    const int k = j | (1 << U);
+    if (GEN == 1) acc += im_cdot(w[j], v[k]) + im_cdot(w[k], v[j]);   // X
+    else acc += re_cdot(w[k], v[j]) - re_cdot(w[j], v[k]);            // Y
+  }
+  return acc;
+}
+// the same for G = Z: amplitude j counts with sign -1 when its target bit is set, that
+// bit being bit j of `bits` (a register bit) or `tbit` for every j (a bit outside them)
+template <typename T>
+__device__ __forceinline__ typename real_of<T>::type grad_z(const T (&v)[16], const T (&w)[16], unsigned bits,
+                                                           int tbit) {
+  typename real_of<T>::type acc = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    const auto x = im_cdot(w[j], v[j]);
+    acc += ((int)((bits >> j) & 1u) | tbit) ? -x : x;
+  }
+  return acc;
+}
+
 }  // namespace sv

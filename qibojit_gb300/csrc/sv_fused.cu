@@ -1523,6 +1523,7 @@ int sv_pass_layout(int dtype, int64_t* offsets, int n) {
 int sv_program_destroy(sv_program* prog) {
   if (prog && prog->spec) specialized_free(prog->spec);
   if (prog && prog->bspec) specialized_free(prog->bspec);
+  if (prog && prog->aspec) specialized_free(prog->aspec);
   delete prog;
   return SV_OK;
 }
@@ -2026,32 +2027,6 @@ static_assert(kAdjMaxGrad >= kMaxPassOpsRefill, "one gradient slot per op of an 
 static_assert(sizeof(PassParams<c128>) + sizeof(AdjArgs<c128>) <= 32764, "adjoint pass parameters");
 static_assert(sizeof(PassParams<c128>) + sizeof(BatchArgs<c128>) + sizeof(void*) <= 32764, "pass parameters");
 
-// products in the state's own precision (FP32 for complex64, FP64 for complex128);
-// block and circuit sums are FP64
-template <typename T>
-__device__ __forceinline__ typename real_of<T>::type im_cdot(T a, T b) {  // Im(conj(a) b)
-  if constexpr (is_complex<T>::value) return a.re * b.im - a.im * b.re;
-  else return 0;
-}
-template <typename T>
-__device__ __forceinline__ typename real_of<T>::type re_cdot(T a, T b) {  // Re(conj(a) b)
-  if constexpr (is_complex<T>::value) return a.re * b.re + a.im * b.im;
-  else return a * b;
-}
-
-template <typename T, int U, int GEN>
-__device__ __forceinline__ typename real_of<T>::type grad_pairs(const T (&v)[16], const T (&w)[16]) {
-  typename real_of<T>::type acc = 0;
-#pragma unroll
-  for (int j = 0; j < 16; j++) {
-    if (j & (1 << U)) continue;
-    const int k = j | (1 << U);
-    if (GEN == 1) acc += im_cdot(w[j], v[k]) + im_cdot(w[k], v[j]);   // X
-    else acc += re_cdot(w[k], v[j]) - re_cdot(w[j], v[k]);            // Y
-  }
-  return acc;
-}
-
 template <typename T, int GEN>
 __device__ __forceinline__ typename real_of<T>::type grad_dispatch(const T (&v)[16], const T (&w)[16], int u) {
   switch (u) {
@@ -2459,6 +2434,10 @@ static int adjoint_run_typed(Context* ctx, sv_adjoint* A, double h, double* ener
     args.ncirc = nc;
     const int threads = 1 << (sg.fwd->kt - kRB);
     for (const Segment& seg : sg.fwd->segments) {
+      if (sg.fwd->bspec) {
+        SV_TRY(specialized_launch_batched(ctx, sg.fwd, seg.pass, st, (void*)psi, sg.d_fcoef, args.coef_stride, nc));
+        continue;
+      }
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(sg.fwd->passes.data() + (size_t)seg.pass * sg.fwd->pass_bytes);
       SV_TRY(launch_pass<T, true>(ctx, p, nullptr, threads, pass_smem<T>(sg.fwd->kt), p.ntiles * nc, st, args));
@@ -2500,6 +2479,11 @@ static int adjoint_run_typed(Context* ctx, sv_adjoint* A, double h, double* ener
     a.gstride = A->gstride;
     const int threads = 1 << (sg.bwd->kt - kRB);
     for (const Segment& seg : sg.bwd->segments) {
+      if (sg.bwd->aspec) {
+        SV_TRY(specialized_launch_adjoint(ctx, sg.bwd, seg.pass, (void*)psi, (void*)lam, sg.d_bcoef, a.coef_stride, nc,
+                                          A->d_gpart, A->nparams, A->gstride));
+        continue;
+      }
       const PassParams<T>& p =
           *reinterpret_cast<const PassParams<T>*>(sg.bwd->passes.data() + (size_t)seg.pass * sg.bwd->pass_bytes);
       if constexpr (sizeof(T) >= 16) SV_TRY(launch_adj<T, 256, 1>(ctx, p, a, threads));
@@ -2682,6 +2666,16 @@ int sv_adjoint_run(sv_context* ctx, sv_adjoint* A, double h, double* energies, d
   if (!ctx || !A) return set_error(SV_ERR_ARG, "null context or adjoint");
   return A->dtype == SV_C128 ? adjoint_run_typed<c128>(ctx, A, h, energies, grads)
                              : adjoint_run_typed<c64>(ctx, A, h, energies, grads);
+}
+
+int sv_adjoint_specialize(sv_context* ctx, sv_adjoint* A) {
+  if (!ctx || !A) return set_error(SV_ERR_ARG, "null context or adjoint");
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  for (auto& sg : A->segs) {
+    SV_TRY(specialize_batched(ctx, sg.fwd, false));
+    SV_TRY(specialize_adjoint(ctx, sg.bwd));
+  }
+  return SV_OK;
 }
 
 int sv_adjoint_state(const sv_adjoint* A, int circuit, void** psi) {

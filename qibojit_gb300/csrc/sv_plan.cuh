@@ -132,6 +132,7 @@ struct sv_program {
   sv::Specialized* spec = nullptr;
   // batched pass kernels for a group of circuits of this structure (sv_batch_specialize)
   sv::Specialized* bspec = nullptr;
+  sv::Specialized* aspec = nullptr;   // adjoint-sweep kernels of a backward program
 };
 
 
@@ -156,6 +157,14 @@ int specialize_batched(Context* ctx, sv_program* prog, bool dw);
 // launches batched pass `pass` over ncirc circuits: state pointer table, coefficient blocks
 int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, cudaStream_t stream, void* states,
                                const void* coef, int64_t coef_stride, int ncirc);
+// compiles the adjoint-sweep kernels of a backward program (psi and lambda, gradient
+// markers) into prog->aspec
+int specialize_adjoint(Context* ctx, sv_program* prog);
+// launches adjoint pass `pass` over ncirc circuits: psi and lambda pointer tables,
+// coefficient blocks, per-block gradient partials gpart[circuit][parameter][gstride]
+int specialized_launch_adjoint(Context* ctx, const sv_program* prog, int pass, void* psis, void* lams,
+                               const void* coef, int64_t coef_stride, int ncirc, double* gpart, int nparams,
+                               int gstride);
 void specialized_free(Specialized* s);
 
 }  // namespace sv

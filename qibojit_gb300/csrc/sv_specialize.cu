@@ -165,10 +165,32 @@ struct KernelShape {
   size_t smem;
 };
 
+// what a generated pass kernel runs over: one state, a batch of states, or the
+// adjoint sweep's psi and lambda states of a batch together with gradient markers
+enum PassMode { PASS_SINGLE = 0, PASS_BATCHED = 1, PASS_ADJOINT = 2 };
+
+// gradient slots an adjoint pass accumulates into (the markers' slot numbers)
 template <typename T>
-KernelShape shape_of(int kt) {
+int adjoint_slots(const PassParams<T>& p) {
+  int ng = 0;
+  for (int q = 0; q < p.nops; q++) {
+    const FOp& f = p.ops[q];
+    if (f.type == FOP_GRADX || f.type == FOP_GRADY || f.type == FOP_GRADZ) ng = std::max(ng, (int)f.u1 + 1);
+  }
+  return ng;
+}
+
+template <typename T>
+KernelShape shape_of(int kt, int mode = PASS_SINGLE, int nslots = 0) {
   KernelShape k;
   k.threads = 1 << (kt - kRB);
+  if (mode == PASS_ADJOINT) {
+    // psi and lambda tiles, both double-buffered, and one FP64 slot per warp and marker
+    k.smem = 4 * sizeof(T) * (size_t)tile_stride(1 << kt) + sizeof(double) * (size_t)nslots * (k.threads / 32);
+    k.maxt = k.threads;
+    k.minb = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(227 * 1024) / k.smem));
+    return k;
+  }
   k.maxt = k.threads <= 256 ? 256 : 512;
   k.minb = (sizeof(T) < 16 && k.threads <= 256) ? 3 : 1;  // the interpreted pass's launch variants
   k.smem = 2 * sizeof(T) * (size_t)tile_stride(1 << kt);
@@ -179,8 +201,15 @@ KernelShape shape_of(int kt) {
 // A batched pass (a group of circuits of one structure) runs over (circuit, tile) items
 // instead, with each circuit's state from a pointer table and its coefficients from its
 // block of a device array (coef_stride elements apart, the pass's own at coef_goff).
+// An adjoint pass is a batched pass over two states per circuit, psi and lambda, that
+// applies every op to both and evaluates the gradient markers between them: each
+// marker's Im<lambda|G|psi> is summed over a warp in the state's precision, over warps
+// and tiles in FP64 shared-memory slots, and written per block and circuit to gpart
+// (the interpreted adjoint pass's layout and order of summation across warps).
 template <typename T>
-std::string pass_source(const PassParams<T>& p, const char* name, bool batched = false) {
+std::string pass_source(const PassParams<T>& p, const char* name, int mode = PASS_SINGLE) {
+  const bool batched = mode != PASS_SINGLE, adj = mode == PASS_ADJOINT;
+  if (adj && stored_as_double_pairs<T>::value) return std::string();  // adjoint: complex64 and complex128 only
   std::ostringstream o;
   const char* ty = stored_as_double_pairs<T>::value ? "sv::cw" : (sizeof(T) == 16 ? "sv::c128" : "sv::c64");
   // double-word passes convert the tile to float pairs in place once it has arrived
@@ -189,7 +218,8 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
                            "    __syncthreads();\n"
                          : "";
   const int kt = p.kt, n = p.n;
-  const KernelShape ks = shape_of<T>(kt);
+  const int nslots = adj ? adjoint_slots(p) : 0;
+  const KernelShape ks = shape_of<T>(kt, mode, nslots);
   const int nth = ks.threads;
   int ncoef = 1;
   for (int q = 0; q < p.nops; q++) ncoef = std::max(ncoef, coef_count(p.ops[q]));
@@ -198,7 +228,12 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
     if (std::find(tpos.begin(), tpos.end(), g) == tpos.end()) outer.push_back(g);
   const std::vector<int> low(tpos.begin(), tpos.begin() + (kt - kRB));
   const char* CF = batched ? "C" : "cf.c";  // where the ops read their coefficients
-  if (batched)
+  if (adj)
+    o << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
+      << "* const* __restrict__ psis, " << ty << "* const* __restrict__ lams, const " << ty
+      << "* __restrict__ coefs, long long coef_stride, int ncirc, double* __restrict__ gpart, int nparams, "
+         "int gstride) {\n";
+  else if (batched)
     o << "extern \"C\" __global__ void __launch_bounds__(" << ks.maxt << ", " << ks.minb << ") " << name << "(" << ty
       << "* const* __restrict__ states, const " << ty << "* __restrict__ coefs, long long coef_stride, int ncirc) {\n";
   else
@@ -224,7 +259,79 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
   // disjoint bits of tid and k * threads
   o << "  constexpr int POSK[16] = {";
   for (int k = 0; k < 16; k++) o << smem_pos(k * nth) << (k < 15 ? ", " : "};\n");
-  if (batched) {
+  if (adj) {
+    const int tshift = n - kt;
+    o << "  using R = sv::real_of<T>::type;\n"
+      << "  constexpr int NW = " << nth / 32 << ";\n"
+      << "  const int warp = tid >> 5, lane = tid & 31;\n"
+      << "  (void)warp;\n  (void)lane;\n";
+    if (nslots > 0) {
+      std::vector<int> param(nslots, -1);
+      for (int q = 0; q < p.nops; q++) {
+        const FOp& f = p.ops[q];
+        if (f.type == FOP_GRADX || f.type == FOP_GRADY || f.type == FOP_GRADZ) param[f.u1] = (int)f.coef;
+      }
+      o << "  constexpr int NG = " << nslots << ";\n"
+        << "  constexpr int PARAM[NG] = {";
+      for (int g = 0; g < nslots; g++) o << param[g] << (g + 1 < nslots ? ", " : "};\n");
+      o << "  double* const gacc = reinterpret_cast<double*>(buf0 + 4 * TSTRIDE);  // [slot][warp]\n"
+        << "  for (int i = tid; i < NG * NW; i += " << nth << ") gacc[i] = 0.0;\n"
+        << "  __syncthreads();\n"
+        // this block's sums of one circuit, then the slots cleared
+        << "  auto flush_grads = [&](int circ) {\n"
+        << "    __syncthreads();\n"
+        << "    for (int g = tid; g < NG; g += " << nth << ") {\n"
+        << "      if (PARAM[g] < 0) continue;\n"
+        << "      double s = 0.0;\n"
+        << "      for (int w = 0; w < NW; w++) {\n"
+        << "        s += gacc[g * NW + w];\n"
+        << "        gacc[g * NW + w] = 0.0;\n"
+        << "      }\n"
+        << "      gpart[((long long)circ * nparams + PARAM[g]) * gstride + blockIdx.x] = s;\n"
+        << "    }\n"
+        << "    __syncthreads();\n"
+        << "  };\n";
+    } else {
+      o << "  auto flush_grads = [&](int) {};\n"
+        << "  (void)gpart;\n  (void)nparams;\n  (void)gstride;\n";
+    }
+    o << "  const long long nitems = " << p.ntiles << "ll * ncirc;\n"
+      << "  auto origin = [&](long long it) -> long long { const long long t = it & " << (p.ntiles - 1) << "ll; return "
+      << deposit_expr("t", outer, true) << "; };\n"
+      << "  auto issue_load = [&](int slot, long long it) {\n"
+      << "    const long long base = origin(it);\n"
+      << "    const T* const sp = psis[it >> " << tshift << "];\n"
+      << "    const T* const sl = lams[it >> " << tshift << "];\n"
+      << "#pragma unroll\n"
+      << "    for (int k = 0; k < 16; k++) {\n"
+      << "      sv::cp_async<sizeof(T)>(buf0 + slot * TSTRIDE + stid + POSK[k], sp + (base | dtid | DEPK[k]));\n"
+      << "      sv::cp_async<sizeof(T)>(buf0 + (2 + slot) * TSTRIDE + stid + POSK[k], sl + (base | dtid | DEPK[k]));\n"
+      << "    }\n"
+      << "    sv::cp_async_commit();\n"
+      << "  };\n"
+      << "  long long t = blockIdx.x;\n"
+      << "  if (t < nitems) issue_load(0, t);\n"
+      << "  int cur = 0, cur_circ = -1;\n"
+      << "  for (; t < nitems; t += gridDim.x, cur ^= 1) {\n"
+      << "    const int circ = (int)(t >> " << tshift << ");\n"
+      << "    if (circ != cur_circ) {\n"
+      << "      if (cur_circ >= 0) flush_grads(cur_circ);\n"
+      << "      cur_circ = circ;\n"
+      << "    }\n"
+      << "    T* const tile = buf0 + cur * TSTRIDE;\n"
+      << "    T* const ltile = buf0 + (2 + cur) * TSTRIDE;\n"
+      << "    const long long base = origin(t);\n"
+      << "    const T* const C = coefs + (long long)circ * coef_stride + " << p.coef_goff << ";\n"
+      << "    (void)C;\n"
+      << "    const long long tn = t + gridDim.x;\n"
+      << "    if (tn < nitems) {\n"
+      << "      issue_load(cur ^ 1, tn);\n"
+      << "      sv::cp_async_wait<1>();\n"
+      << "    } else {\n"
+      << "      sv::cp_async_wait<0>();\n"
+      << "    }\n"
+      << "    __syncthreads();\n";
+  } else if (batched) {
     const int tshift = n - kt;
     o << "  const long long nitems = " << p.ntiles << "ll * ncirc;\n"
       << "  auto origin = [&](long long it) -> long long { const long long t = it & " << (p.ntiles - 1) << "ll; return "
@@ -276,6 +383,8 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "    }\n"
       << "    __syncthreads();\n" << conv;
   }
+  // the register arrays every op applies to: the state, or psi and lambda
+  const std::vector<std::string> arrs = adj ? std::vector<std::string>{"v", "w"} : std::vector<std::string>{"v"};
   for (int ph = 0; ph < p.nphases; ph++) {
     const Phase& P = p.phases[ph];
     std::vector<int> nonreg;
@@ -289,6 +398,11 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       << "      T* const tp = tile + lbase + (lbase >> 4) + (lbase >> 8);\n"
       << "      T v[16];\n";
     for (int j = 0; j < 16; j++) o << "      v[" << j << "] = tp[" << P.soff[j] << "];\n";
+    if (adj) {
+      o << "      T* const tq = ltile + lbase + (lbase >> 4) + (lbase >> 8);\n"
+        << "      T w[16];\n";
+      for (int j = 0; j < 16; j++) o << "      w[" << j << "] = tq[" << P.soff[j] << "];\n";
+    }
     bool uses_pn = false;
     for (int q = P.op_begin; q < P.op_end; q++) uses_pn |= p.ops[q].type == FOP_SIGN;
     if (uses_pn) o << "      unsigned pn = 0;\n";
@@ -296,10 +410,32 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
     bool dyn = false;   // run-time negations pending in pn
     auto flush = [&]() {
       for (int j = 0; j < 16; j++)
-        if ((stat >> j) & 1) o << "      v[" << j << "] = sv::tneg(v[" << j << "]);\n";
+        if ((stat >> j) & 1)
+          for (const std::string& a : arrs) o << "      " << a << "[" << j << "] = sv::tneg(" << a << "[" << j << "]);\n";
       stat = 0;
-      if (dyn) o << "      sv::apply_negations(v, pn);\n      pn = 0;\n";
+      if (dyn) {
+        for (const std::string& a : arrs) o << "      sv::apply_negations(" << a << ", pn);\n";
+        o << "      pn = 0;\n";
+      }
       dyn = false;
+    };
+    // one statement per register array, under the op's condition when it has one
+    auto each = [&](const std::string& pre, auto&& stmt) {
+      if (arrs.size() == 1) {
+        o << pre << stmt(arrs[0]) << "\n";
+        return;
+      }
+      o << pre << "{\n";
+      for (const std::string& a : arrs) o << "        " << stmt(a) << "\n";
+      o << "      }\n";
+    };
+    // a gradient marker's warp sum, added to its FP64 slot by the warp's first lane
+    auto grad_sum = [&](const FOp& f, const std::string& expr) {
+      o << "      {\n        R g = " << expr << ";\n"
+        << "#pragma unroll\n"
+        << "        for (int off = 16; off > 0; off >>= 1) g += __shfl_xor_sync(0xffffffffu, g, off);\n"
+        << "        if (lane == 0) gacc[" << (int)f.u1 << " * NW + warp] += (double)g;\n"
+        << "      }\n";
     };
     // the thread / tile control test of an op, and the non-register part of a diagonal's
     // table index (empty when the op has none)
@@ -337,45 +473,69 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
       const std::string cond = cond_of(f);
       const std::string pre = cond.empty() ? "      " : "      if (" + cond + ") ";
       if (f.type == FOP_D1RUN || f.type == FOP_D1RUNR || f.type == FOP_DENSE1 || f.type == FOP_DENSE1R ||
-          f.type == FOP_DENSE1P || f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2)
+          f.type == FOP_DENSE1P || f.type == FOP_X1 || f.type == FOP_SWAP2 || f.type == FOP_DENSE2 ||
+          f.type == FOP_GRADX || f.type == FOP_GRADY)
         flush();
       const std::string tix = index_of(f);
       const bool tany = !tix.empty();
       std::ostringstream te;
       te << tix;
+      const std::string cf = std::string(CF) + " + ";
       switch (f.type) {
         case FOP_D1RUN:
           for (int k = 0; k < f.nrun; k++)
-            o << "      sv::dense1_regs<T, " << (int)f.ru[k] << ">(v, " << CF << " + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+            each("      ", [&](const std::string& a) {
+              return "sv::dense1_regs<T, " + std::to_string((int)f.ru[k]) + ">(" + a + ", " + cf +
+                     std::to_string(f.coef + 4 * k) + ", 0xffffu);";
+            });
           break;
         case FOP_D1RUNR:
           for (int k = 0; k < f.nrun; k++)
-            o << "      sv::dense1r_regs<T, " << (int)f.ru[k] << ">(v, " << CF << " + " << (f.coef + 4 * k) << ", 0xffffu);\n";
+            each("      ", [&](const std::string& a) {
+              return "sv::dense1r_regs<T, " + std::to_string((int)f.ru[k]) + ">(" + a + ", " + cf +
+                     std::to_string(f.coef + 4 * k) + ", 0xffffu);";
+            });
           break;
         case FOP_DIAGR:  // commutes with the pending sign flips
           for (int j = 0; j < 16; j++)
-            o << "      v[" << j << "] = sv::tmul(" << CF << "[" << (f.coef + j) << "], v[" << j << "]);\n";
+            for (const std::string& a : arrs)
+              o << "      " << a << "[" << j << "] = sv::tmul(" << CF << "[" << (f.coef + j) << "], " << a << "[" << j
+                << "]);\n";
           break;
         case FOP_DENSE1:
-          o << pre << "sv::dense1_regs<T, " << (int)f.u0 << ">(v, " << CF << " + " << f.coef << ", " << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::dense1_regs<T, " + std::to_string((int)f.u0) + ">(" + a + ", " + cf + std::to_string(f.coef) +
+                   ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_DENSE1P:
-          o << pre << "sv::pivot1_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, " << CF << " + " << f.coef << ", "
-            << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::pivot1_regs<T, " + std::to_string((int)f.u0) + ", " + std::to_string((int)f.u1) + ">(" + a +
+                   ", " + cf + std::to_string(f.coef) + ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_DENSE1R:
-          o << pre << "sv::dense1r_regs<T, " << (int)f.u0 << ">(v, " << CF << " + " << f.coef << ", " << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::dense1r_regs<T, " + std::to_string((int)f.u0) + ">(" + a + ", " + cf + std::to_string(f.coef) +
+                   ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_X1:
-          o << pre << "sv::x1_regs<T, " << (int)f.u0 << ">(v, " << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::x1_regs<T, " + std::to_string((int)f.u0) + ">(" + a + ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_SWAP2:
-          o << pre << "sv::swap2_regs<T, " << (int)std::min(f.u0, f.u1) << ", " << (int)std::max(f.u0, f.u1) << ">(v, "
-            << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::swap2_regs<T, " + std::to_string((int)std::min(f.u0, f.u1)) + ", " +
+                   std::to_string((int)std::max(f.u0, f.u1)) + ">(" + a + ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_DENSE2:
-          o << pre << "sv::dense2_regs<T, " << (int)f.u0 << ", " << (int)f.u1 << ">(v, " << CF << " + " << f.coef << ", "
-            << f.jmask << "u);\n";
+          each(pre, [&](const std::string& a) {
+            return "sv::dense2_regs<T, " + std::to_string((int)f.u0) + ", " + std::to_string((int)f.u1) + ">(" + a +
+                   ", " + cf + std::to_string(f.coef) + ", " + std::to_string(f.jmask) + "u);";
+          });
           break;
         case FOP_SIGN:
           if (!tany && cond.empty()) {
@@ -404,7 +564,9 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
             for (int j = 0; j < 16; j++) {
               if (!((f.jmask >> j) & 1)) continue;
               const int r = (int)((f.rpart >> (4 * j)) & 15);
-              o << "        v[" << j << "] = sv::tmul(" << CF << "[" << f.coef << " + (" << r << " | ti)], v[" << j << "]);\n";
+              for (const std::string& a : arrs)
+                o << "        " << a << "[" << j << "] = sv::tmul(" << CF << "[" << f.coef << " + (" << r << " | ti)], "
+                  << a << "[" << j << "]);\n";
             }
             o << "      }\n";
             break;
@@ -430,18 +592,49 @@ std::string pass_source(const PassParams<T>& p, const char* name, bool batched =
             if (!((f.jmask >> j) & 1)) continue;
             const int r = (int)((f.rpart >> (4 * j)) & 15);
             const size_t k = std::find(rs.begin(), rs.end(), r) - rs.begin();
-            o << "        v[" << j << "] = sv::tmul(fr" << k << ", v[" << j << "]);\n";
+            for (const std::string& a : arrs) o << "        " << a << "[" << j << "] = sv::tmul(fr" << k << ", " << a << "[" << j << "]);\n";
           }
           o << "      }\n";
           break;
         }
+        case FOP_GRADX:
+        case FOP_GRADY:
+          if (!adj) return std::string();
+          grad_sum(f, "sv::grad_pairs<T, " + std::to_string((int)f.u0) + ", " + (f.type == FOP_GRADX ? "1" : "2") +
+                          ">(v, w)");
+          break;
+        case FOP_GRADZ: {  // invariant under the pending sign flips (both states carry them)
+          if (!adj) return std::string();
+          unsigned bits = 0;
+          for (int j = 0; j < 16; j++) bits |= (unsigned)((f.rpart >> (4 * j)) & 1) << j;
+          std::string tbit = "0";
+          if (f.tb[0] >= 0) tbit = "((lbase >> " + std::to_string((int)f.tb[0]) + ") & 1)";
+          else if (f.ob[0] >= 0) tbit = "(int)((base >> " + std::to_string((int)f.ob[0]) + ") & 1)";
+          grad_sum(f, "sv::grad_z<T>(v, w, " + std::to_string(bits) + "u, " + tbit + ")");
+          break;
+        }
         default:
-          return std::string();  // gradient markers and anything else: not specialisable
+          return std::string();  // anything else: not specialisable
       }
     }
     flush();
     for (int j = 0; j < 16; j++) o << "      tp[" << P.soff[j] << "] = v[" << j << "];\n";
+    if (adj)
+      for (int j = 0; j < 16; j++) o << "      tq[" << P.soff[j] << "] = w[" << j << "];\n";
     o << "      __syncthreads();\n    }\n";
+  }
+  if (adj) {
+    o << "    T* const sp = psis[circ];\n"
+      << "    T* const sl = lams[circ];\n"
+      << "#pragma unroll\n"
+      << "    for (int k = 0; k < 16; k++) {\n"
+      << "      sv::stg_stream(sp + (base | dtid | DEPK[k]), tile[stid + POSK[k]]);\n"
+      << "      sv::stg_stream(sl + (base | dtid | DEPK[k]), ltile[stid + POSK[k]]);\n"
+      << "    }\n"
+      << "    __syncthreads();  // these buffers are refilled by the prefetch two tiles later\n"
+      << "  }\n"
+      << "  if (cur_circ >= 0) flush_grads(cur_circ);\n}\n";
+    return o.str();
   }
   o << "#pragma unroll\n"
     << "    for (int k = 0; k < 16; k++) sv::stg_stream(" << (batched ? "st" : "state")
@@ -594,15 +787,17 @@ bool specialized_is_dw(const Specialized* s) { return s && s->dw; }
 void specialized_free(Specialized* s) { delete s; }
 
 // generates, compiles (in parallel, through the process cache) and loads the pass
-// kernels of a program, single-state or batched
+// kernels of a program: single-state, batched or adjoint (PassMode)
 template <typename T>
-static int build_kernels(Context* ctx, const sv_program* prog, bool batched, std::unique_ptr<Specialized>* out) {
+static int build_kernels(Context* ctx, const sv_program* prog, int mode, std::unique_ptr<Specialized>* out) {
   const int np = prog->npasses;
-  const char* name = batched ? "sv_bpass" : "sv_pass";
+  const char* name = mode == PASS_ADJOINT ? "sv_apass" : mode == PASS_BATCHED ? "sv_bpass" : "sv_pass";
+  auto block = [&](int i) -> const PassParams<T>& {
+    return *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)i * prog->pass_bytes);
+  };
   std::vector<std::string> sources(np);
   for (int i = 0; i < np; i++) {
-    const PassParams<T>& p = *reinterpret_cast<const PassParams<T>*>(prog->passes.data() + (size_t)i * prog->pass_bytes);
-    sources[i] = pass_source<T>(p, name, batched);
+    sources[i] = pass_source<T>(block(i), name, mode);
     if (sources[i].empty()) return set_error(SV_ERR_UNSUPPORTED, "pass %d holds ops that cannot be specialised", i);
   }
   // compile the sources not in the cache, in parallel
@@ -655,8 +850,8 @@ static int build_kernels(Context* ctx, const sv_program* prog, bool batched, std
   }
   std::unique_ptr<Specialized> s(new Specialized());
   s->passes.resize(np);
-  const KernelShape ks = shape_of<T>(prog->kt);
   for (int i = 0; i < np; i++) {
+    const KernelShape ks = shape_of<T>(prog->kt, mode, mode == PASS_ADJOINT ? adjoint_slots(block(i)) : 0);
     PassKernel& pk = s->passes[i];
     {
       std::lock_guard<std::mutex> g(g_cache_mutex);
@@ -684,10 +879,10 @@ static int specialize_typed(Context* ctx, sv_program* prog) {
   SV_TRY(refold_program(prog));
   std::unique_ptr<Specialized> s;
   if (std::is_same<T, c128>::value && !ctx->c128_fp64) {  // complex128 in double-word arithmetic
-    SV_TRY(build_kernels<cw>(ctx, prog, false, &s));
+    SV_TRY(build_kernels<cw>(ctx, prog, PASS_SINGLE, &s));
     s->dw = true;
   } else {
-    SV_TRY(build_kernels<T>(ctx, prog, false, &s));
+    SV_TRY(build_kernels<T>(ctx, prog, PASS_SINGLE, &s));
   }
   if (prog->spec) specialized_free(prog->spec);
   prog->spec = s.release();
@@ -702,10 +897,11 @@ int specialize_batched(Context* ctx, sv_program* prog, bool dw) {
   if (prog->fold_diagonals) return set_error(SV_ERR_ARG, "batched passes need an unfolded program");
   std::unique_ptr<Specialized> s;
   if (prog->dtype == SV_C128 && dw) {
-    SV_TRY(build_kernels<cw>(ctx, prog, true, &s));
+    SV_TRY(build_kernels<cw>(ctx, prog, PASS_BATCHED, &s));
     s->dw = true;
   } else {
-    SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, true, &s) : build_kernels<c64>(ctx, prog, true, &s));
+    SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, PASS_BATCHED, &s)
+                                   : build_kernels<c64>(ctx, prog, PASS_BATCHED, &s));
   }
   if (prog->bspec) specialized_free(prog->bspec);
   prog->bspec = s.release();
@@ -723,6 +919,34 @@ int specialized_launch_batched(Context* ctx, const sv_program* prog, int pass, c
   SV_TRY(check_cuda(cudaLaunchKernel((const void*)pk.kernel, dim3((unsigned)grid), dim3(pk.threads), args, pk.smem,
                                      stream),
                     "specialised batched pass launch"));
+  return SV_OK;
+}
+
+int specialize_adjoint(Context* ctx, sv_program* prog) {
+  if (!nvrtc().ok)
+    return set_error(SV_ERR_UNSUPPORTED, "the CUDA runtime compiler (libnvrtc.so.13) could not be loaded");
+  if (prog->fold_diagonals) return set_error(SV_ERR_ARG, "adjoint passes need an unfolded program");
+  std::unique_ptr<Specialized> s;
+  SV_TRY(prog->dtype == SV_C128 ? build_kernels<c128>(ctx, prog, PASS_ADJOINT, &s)
+                                : build_kernels<c64>(ctx, prog, PASS_ADJOINT, &s));
+  if (prog->aspec) specialized_free(prog->aspec);
+  prog->aspec = s.release();
+  return SV_OK;
+}
+
+int specialized_launch_adjoint(Context* ctx, const sv_program* prog, int pass, void* psis, void* lams,
+                               const void* coef, int64_t coef_stride, int ncirc, double* gpart, int nparams,
+                               int gstride) {
+  const PassKernel& pk = prog->aspec->passes[pass];
+  const int64_t items = ((int64_t)1 << (prog->nqubits - prog->kt)) * ncirc;
+  int64_t grid = (int64_t)pk.per_sm * ctx->num_sms;
+  if (grid > items) grid = items;
+  if (grid > gstride) grid = gstride;  // one gradient column per block
+  long long stride = (long long)coef_stride;
+  void* args[] = {&psis, &lams, const_cast<void**>(&coef), &stride, &ncirc, &gpart, &nparams, &gstride};
+  SV_TRY(check_cuda(cudaLaunchKernel((const void*)pk.kernel, dim3((unsigned)grid), dim3(pk.threads), args, pk.smem,
+                                     ctx->stream),
+                    "specialised adjoint pass launch"));
   return SV_OK;
 }
 

@@ -215,3 +215,83 @@ def test_fixed_complex_gates_inside_adjoint_circuits(backend, dt):
         pm[layer, q, k] -= np.pi / 2
         shift = (oracle_energy(pp) - oracle_energy(pm)) / 2
         assert abs(G[layer, q, k] - shift) < tol_g, (layer, q, k, G[layer, q, k], shift)
+
+
+def test_adjoint_n26_l20_against_parameter_shift_and_complex128(backend):
+    """The benchmarked configuration (n=26, 20 layers, 1040 parameters per circuit,
+    checkpoints every 5 layers): complex64 adjoint gradients and energies against the
+    complex128 adjoint on every parameter, and the complex128 adjoint against parameter
+    shift on six parameters spread over the circuit (the shifted energies from batched
+    complex128 circuits in FP64 arithmetic)."""
+    from qibojit_gb300.adjoint import AdjointTFIM
+    from qibojit_gb300.batch import BatchedCircuits
+
+    n, L, nc = 26, 20, 2
+    p = np.random.default_rng(21).uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    res = {}
+    for dt in ("complex64", "complex128"):
+        eng = AdjointTFIM(backend, n, L, nc, dt, checkpoint_every=5)
+        res[dt] = eng(p)
+        eng.close()
+    (E64, G64), (E128, G128) = res["complex64"], res["complex128"]
+    assert np.abs(E64 - E128).max() < 1e-6
+    assert np.abs(G64 - G128).max() < 1e-6
+    picks = [(0, 0, 0), (0, 25, 1), (7, 13, 0), (12, 4, 1), (19, 25, 0), (19, 0, 1)]
+    specs = []
+    for layer, q, k in picks:
+        for sgn in (1, -1):
+            pp = p[0].copy()
+            pp[layer, q, k] += sgn * np.pi / 2
+            specs.append((n, L, pp))
+    backend.ctx.set_c128_arithmetic("fp64")
+    try:
+        bat = BatchedCircuits.from_hea(backend, specs, "complex128")
+    finally:
+        backend.ctx.set_c128_arithmetic("double-word")
+    bat.run()
+    en = bat.tfim_energies(1.0)
+    bat.close()
+    for i, (layer, q, k) in enumerate(picks):
+        shift = (en[2 * i] - en[2 * i + 1]) / 2
+        assert abs(G128[0, layer, q, k] - shift) < 1e-10, (layer, q, k, G128[0, layer, q, k], shift)
+
+
+@pytest.mark.parametrize("dt,tol", [("complex128", 1e-12), ("complex64", 2e-5)])
+@pytest.mark.parametrize("n,L,every", [(9, 3, 2), (12, 4, 1), (14, 5, 5)])
+def test_specialised_adjoint_matches_interpreted(backend, dt, tol, n, L, every):
+    """sv_adjoint_specialize: forward and reverse-sweep passes compiled with the
+    structure and every gradient marker as literals give the interpreting kernels'
+    energies and gradients, also after new parameters (sv_adjoint_update)."""
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    nc = 3
+    rng = np.random.default_rng(40 + n)
+    p1 = rng.uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    p2 = rng.uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    spec = AdjointTFIM(backend, n, L, nc, dt, checkpoint_every=every, specialize=True)
+    ref = AdjointTFIM(backend, n, L, nc, dt, checkpoint_every=every)
+    for p in (p1, p2):
+        Es, Gs = spec(p)
+        Er, Gr = ref(p)
+        np.testing.assert_allclose(Es, Er, rtol=0, atol=tol)
+        np.testing.assert_allclose(Gs, Gr, rtol=0, atol=tol)
+    spec.close()
+    ref.close()
+
+
+def test_specialised_adjoint_matches_parameter_shift(backend):
+    from qibojit_gb300.adjoint import AdjointTFIM
+
+    n, L, nc = 9, 3, 2
+    params = np.random.default_rng(11).uniform(0, 2 * np.pi, size=(nc, L, n, 2))
+    eng = AdjointTFIM(backend, n, L, nc, "complex128", h=1.0, checkpoint_every=2, specialize=True)
+    E, G = eng(params)
+    eng.close()
+    for c in range(nc):
+        assert abs(E[c] - oracle_energy(n, L, params[c])[0]) < 1e-11
+        for (layer, q, k) in [(0, 0, 0), (0, 8, 1), (1, 3, 0), (2, 5, 1)]:
+            pp, pm = params[c].copy(), params[c].copy()
+            pp[layer, q, k] += np.pi / 2
+            pm[layer, q, k] -= np.pi / 2
+            shift = (oracle_energy(n, L, pp)[0] - oracle_energy(n, L, pm)[0]) / 2
+            assert abs(G[c, layer, q, k] - shift) < 1e-10
