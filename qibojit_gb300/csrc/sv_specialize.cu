@@ -185,8 +185,10 @@ KernelShape shape_of(int kt, int mode = PASS_SINGLE, int nslots = 0) {
   KernelShape k;
   k.threads = 1 << (kt - kRB);
   if (mode == PASS_ADJOINT) {
-    // psi and lambda tiles, both double-buffered, and one FP64 slot per warp and marker
-    k.smem = 4 * sizeof(T) * (size_t)tile_stride(1 << kt) + sizeof(double) * (size_t)nslots * (k.threads / 32);
+    // psi and lambda tiles, both double-buffered, one FP64 sum per marker and the
+    // current tile's warp sums (the state's real type) per marker and warp
+    k.smem = 4 * sizeof(T) * (size_t)tile_stride(1 << kt) + sizeof(double) * (size_t)nslots +
+             sizeof(T) / 2 * (size_t)nslots * (k.threads / 32);
     k.maxt = k.threads;
     k.minb = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(227 * 1024) / k.smem));
     return k;
@@ -203,9 +205,10 @@ KernelShape shape_of(int kt, int mode = PASS_SINGLE, int nslots = 0) {
 // block of a device array (coef_stride elements apart, the pass's own at coef_goff).
 // An adjoint pass is a batched pass over two states per circuit, psi and lambda, that
 // applies every op to both and evaluates the gradient markers between them: each
-// marker's Im<lambda|G|psi> is summed over a warp in the state's precision, over warps
-// and tiles in FP64 shared-memory slots, and written per block and circuit to gpart
-// (the interpreted adjoint pass's layout and order of summation across warps).
+// marker's Im<lambda|G|psi> is summed over a warp and then over the tile's warps in
+// the state's precision, over tiles in an FP64 shared-memory slot (one FP64 add per
+// marker and tile), and written per block and circuit to gpart (the interpreted
+// adjoint pass's layout).
 template <typename T>
 std::string pass_source(const PassParams<T>& p, const char* name, int mode = PASS_SINGLE) {
   const bool batched = mode != PASS_SINGLE, adj = mode == PASS_ADJOINT;
@@ -274,25 +277,31 @@ std::string pass_source(const PassParams<T>& p, const char* name, int mode = PAS
       o << "  constexpr int NG = " << nslots << ";\n"
         << "  constexpr int PARAM[NG] = {";
       for (int g = 0; g < nslots; g++) o << param[g] << (g + 1 < nslots ? ", " : "};\n");
-      o << "  double* const gacc = reinterpret_cast<double*>(buf0 + 4 * TSTRIDE);  // [slot][warp]\n"
-        << "  for (int i = tid; i < NG * NW; i += " << nth << ") gacc[i] = 0.0;\n"
+      o << "  double* const gacc = reinterpret_cast<double*>(buf0 + 4 * TSTRIDE);  // [slot]\n"
+        << "  R* const gw = reinterpret_cast<R*>(gacc + NG);  // [slot][warp], the current tile's\n"
+        << "  for (int i = tid; i < NG; i += " << nth << ") gacc[i] = 0.0;\n"
+        << "  for (int i = tid; i < NG * NW; i += " << nth << ") gw[i] = 0;\n"
         << "  __syncthreads();\n"
+        // a tile's warp sums into the FP64 slots (after the tile's last barrier)
+        << "  auto add_tile = [&]() {\n"
+        << "    for (int g = tid; g < NG; g += " << nth << ") {\n"
+        << "      R s = gw[g * NW];\n"
+        << "      for (int w = 1; w < NW; w++) s += gw[g * NW + w];\n"
+        << "      gacc[g] += (double)s;\n"
+        << "    }\n"
+        << "  };\n"
         // this block's sums of one circuit, then the slots cleared
         << "  auto flush_grads = [&](int circ) {\n"
         << "    __syncthreads();\n"
         << "    for (int g = tid; g < NG; g += " << nth << ") {\n"
-        << "      if (PARAM[g] < 0) continue;\n"
-        << "      double s = 0.0;\n"
-        << "      for (int w = 0; w < NW; w++) {\n"
-        << "        s += gacc[g * NW + w];\n"
-        << "        gacc[g * NW + w] = 0.0;\n"
-        << "      }\n"
-        << "      gpart[((long long)circ * nparams + PARAM[g]) * gstride + blockIdx.x] = s;\n"
+        << "      if (PARAM[g] >= 0) gpart[((long long)circ * nparams + PARAM[g]) * gstride + blockIdx.x] = gacc[g];\n"
+        << "      gacc[g] = 0.0;\n"
         << "    }\n"
         << "    __syncthreads();\n"
         << "  };\n";
     } else {
-      o << "  auto flush_grads = [&](int) {};\n"
+      o << "  auto add_tile = [&]() {};\n"
+        << "  auto flush_grads = [&](int) {};\n"
         << "  (void)gpart;\n  (void)nparams;\n  (void)gstride;\n";
     }
     o << "  const long long nitems = " << p.ntiles << "ll * ncirc;\n"
@@ -434,7 +443,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, int mode = PAS
       o << "      {\n        R g = " << expr << ";\n"
         << "#pragma unroll\n"
         << "        for (int off = 16; off > 0; off >>= 1) g += __shfl_xor_sync(0xffffffffu, g, off);\n"
-        << "        if (lane == 0) gacc[" << (int)f.u1 << " * NW + warp] += (double)g;\n"
+        << "        if (lane == 0) gw[" << (int)f.u1 << " * NW + warp] = g;\n"
         << "      }\n";
     };
     // the thread / tile control test of an op, and the non-register part of a diagonal's
@@ -632,6 +641,7 @@ std::string pass_source(const PassParams<T>& p, const char* name, int mode = PAS
       << "      sv::stg_stream(sl + (base | dtid | DEPK[k]), ltile[stid + POSK[k]]);\n"
       << "    }\n"
       << "    __syncthreads();  // these buffers are refilled by the prefetch two tiles later\n"
+      << "    add_tile();\n"
       << "  }\n"
       << "  if (cur_circ >= 0) flush_grads(cur_circ);\n}\n";
     return o.str();
