@@ -301,6 +301,16 @@ int sv_batch_run(sv_context* ctx, sv_batch* b);
  * coefficient block); later sv_batch_run calls launch them and record a new graph.
  * Synchronises the device first.  SV_ERR_UNSUPPORTED when libnvrtc is absent. */
 int sv_batch_specialize(sv_context* ctx, sv_batch* b);
+/* How sv_batch_run executes the batch.  SV_BATCH_GRAPH (the default): one launch per
+ * group and pass (interpreting, or the kernels of sv_batch_specialize) spread over four
+ * streams and recorded as one CUDA graph.  SV_BATCH_PERSISTENT: every pass of every
+ * group in one cooperative launch of an interpreting kernel whose blocks take work
+ * tickets in order (each circuit's pass r after its pass r - 1, tracked per circuit in
+ * device counters); recorded as a graph where the driver allows, eager otherwise.  Its
+ * waits are bounded: a wait that runs out stops the launch and the next sv_sync or
+ * sv_batch_tfim_energy returns SV_ERR_TIMEOUT.  Synchronises the batch's streams. */
+enum sv_batch_executor { SV_BATCH_GRAPH = 0, SV_BATCH_PERSISTENT = 1 };
+int sv_batch_set_executor(sv_context* ctx, sv_batch* b, int executor);
 /* Transverse-field Ising energies E_c = -sum_i <Z_i Z_{i+1}> - h sum_i <X_i> (open chain),
  * FP64 accumulation; `energies` (host) receives ncirc values; synchronises. */
 int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energies);

@@ -154,6 +154,17 @@ class BatchedCircuits:
         _lib.check(self.lib.sv_batch_specialize(self.ctx.handle, self._h), "sv_batch_specialize")
         return self
 
+    def set_executor(self, executor: str) -> "BatchedCircuits":
+        """"graph": a launch per group and pass over four streams, recorded as one CUDA
+        graph (the default); "persistent": the whole batch in one cooperative launch of
+        an interpreting kernel (``sv_batch_set_executor``)."""
+        codes = {"graph": 0, "persistent": 1}
+        if executor not in codes:
+            raise ValueError(f"executor must be one of {sorted(codes)}")
+        _lib.check(self.lib.sv_batch_set_executor(self.ctx.handle, self._h, codes[executor]),
+                   "sv_batch_set_executor")
+        return self
+
     def tfim_energies(self, h: float = 1.0) -> np.ndarray:
         out = np.zeros(self.ncirc, dtype=np.float64)
         _lib.check(self.lib.sv_batch_tfim_energy(self.ctx.handle, self._h, float(h), out.ctypes.data),

@@ -82,6 +82,9 @@ int ensure_scratch(Context* ctx, size_t bytes);
 int ensure_host_pinned(Context* ctx, size_t bytes);
 int ensure_operand(Context* ctx, size_t bytes);
 int ensure_device_status(Context* ctx);
+// after the context stream has been synchronised: SV_ERR_TIMEOUT when a kernel with a
+// bounded wait gave up since the last check (the status word is then cleared)
+int take_device_status(Context* ctx);
 
 #define SV_TRY(...)                  \
   do {                               \

@@ -69,6 +69,20 @@ int ensure_operand(Context* ctx, size_t bytes) {
   return SV_OK;
 }
 
+int take_device_status(Context* ctx) {
+  if (!ctx->status_pending) return SV_OK;
+  // kernels with bounded waits report a time-out in the status word: 1 from the
+  // tensor-core gates, 2 from the persistent batch executor
+  ctx->status_pending = false;
+  int status = 0;
+  SV_TRY(check_cuda(cudaMemcpy(&status, ctx->device_status, sizeof(int), cudaMemcpyDeviceToHost), "status word read"));
+  if (status == 0) return SV_OK;
+  SV_TRY(check_cuda(cudaMemset(ctx->device_status, 0, sizeof(int)), "status word reset"));
+  if (status == 2)
+    return set_error(SV_ERR_TIMEOUT, "the persistent batch executor gave up waiting for a circuit's previous pass");
+  return set_error(SV_ERR_TIMEOUT, "a tensor-core gate kernel gave up waiting for its matrix operations");
+}
+
 int ensure_device_status(Context* ctx) {
   if (ctx->device_status) return SV_OK;
   SV_TRY(check_cuda(cudaMalloc(&ctx->device_status, sizeof(int)), "status word allocation"));
@@ -153,18 +167,7 @@ int sv_context_set_c128_arithmetic(sv_context* ctx, int mode) {
 int sv_sync(sv_context* ctx) {
   if (!ctx) return sv::set_error(SV_ERR_ARG, "null context");
   SV_TRY(sv::check_cuda(cudaStreamSynchronize(ctx->stream), "sv_sync"));
-  if (ctx->status_pending) {
-    // kernels with bounded waits (the tensor-core gates) report a time-out here
-    ctx->status_pending = false;
-    int status = 0;
-    SV_TRY(sv::check_cuda(cudaMemcpy(&status, ctx->device_status, sizeof(int), cudaMemcpyDeviceToHost),
-                          "status word read"));
-    if (status != 0) {
-      SV_TRY(sv::check_cuda(cudaMemset(ctx->device_status, 0, sizeof(int)), "status word reset"));
-      return sv::set_error(SV_ERR_TIMEOUT, "a tensor-core gate kernel gave up waiting for its matrix operations");
-    }
-  }
-  return SV_OK;
+  return sv::take_device_status(ctx);
 }
 
 }  // extern "C"

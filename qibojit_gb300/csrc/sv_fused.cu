@@ -138,63 +138,16 @@ struct BatchArgs {
   int32_t pad;
 };
 
-template <typename T, int MAXT, int MINB, bool BATCHED>
-__global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state,
-                                                         const __grid_constant__ PassParams<T> p,
-                                                         const __grid_constant__ BatchArgs<T> batch) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int kt = p.kt;
-  const int tsize = 1 << kt;
-  const int tstride = tile_stride(tsize);
-  T* const buf0 = reinterpret_cast<T*>(smem_raw);  // two tiles, tstride apart
-  int64_t* dep_hi = reinterpret_cast<int64_t*>(buf0 + 2 * tstride);
-  const int nhi = kt - kLowBits;
-  for (int h = threadIdx.x; h < (1 << nhi); h += blockDim.x) {
-    int64_t o = 0;
-    for (int b = 0; b < nhi; b++)
-      if ((h >> b) & 1) o |= (int64_t)1 << p.tile_pos[kLowBits + b];
-    dep_hi[h] = o;
-  }
-  __syncthreads();
-  const int nthreads = blockDim.x;
-  auto issue_load = [&](T* buf, const T* st, int64_t base) {
-    for (int e = threadIdx.x; e < tsize; e += nthreads)
-      cp_async<sizeof(T)>(buf + smem_pos(e), st + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))));
-    cp_async_commit();
-  };
-  // items: (circuit, tile) for batched runs, tiles of the one state otherwise
-  const int64_t nitems = BATCHED ? p.ntiles * batch.ncirc : p.ntiles;
-  const int tshift = p.n - kt;  // ntiles = 2^tshift
-  auto item_state = [&](int64_t it) -> T* {
-    if constexpr (BATCHED) return batch.states[it >> tshift];
-    else return state;
-  };
-  auto item_tile = [&](int64_t it) -> int64_t { return BATCHED ? (it & (p.ntiles - 1)) : it; };
-  int64_t t = blockIdx.x;
-  if (t < nitems) issue_load(buf0, item_state(t), tile_origin(item_tile(t), p.tile_pos, kt));
-  int cur = 0;
-  for (; t < nitems; t += gridDim.x, cur ^= 1) {
-    T* tile = buf0 + cur * tstride;
-    T* const st = item_state(t);
-    const int64_t base = tile_origin(item_tile(t), p.tile_pos, kt);
-    const T* cbase;
-    if constexpr (BATCHED) cbase = batch.coef + (t >> tshift) * batch.coef_stride + p.coef_goff;
-    else cbase = p.coef;
-    const int64_t tn = t + gridDim.x;
-    if (tn < nitems) {
-      issue_load(buf0 + (cur ^ 1) * tstride, item_state(tn), tile_origin(item_tile(tn), p.tile_pos, kt));
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    __syncthreads();
-    if constexpr (stored_as_double_pairs<T>::value) {
-      // the tile arrived as complex128 bytes: convert it to float pairs in place, once
-      // per pass (the final stores convert back)
-      for (int e = threadIdx.x; e < tsize; e += nthreads) cw_from_stored(tile + smem_pos(e));
-      __syncthreads();
-    }
-    for (int ph = 0; ph < p.nphases; ph++) {
+// the ops of one pass on one tile in shared memory, phase by phase (a barrier after
+// each); `active`: this thread holds registers in this tile (threads beyond the tile's
+// 2^(kt-4) only take part in the barriers)
+template <typename T>
+__device__ __forceinline__ void tile_phases(const PassParams<T>& p, T* tile, const T* cbase, int64_t base,
+                                            bool active) {
+  for (int ph = 0; ph < p.nphases; ph++) {
+    // one barrier instruction for every thread (an aligned barrier must not be reached
+    // by the lanes of one warp at different call sites)
+    if (active) {
       const Phase& P = p.phases[ph];
       const int r0 = P.rb[0], r1 = P.rb[1], r2 = P.rb[2], r3 = P.rb[3];
       // thread bits deposited into the non-register local bits (register bits ascending)
@@ -302,8 +255,68 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state
       if (pending_neg) apply_negations(v, pending_neg);
 #pragma unroll
       for (int j = 0; j < 16; j++) tp_base[P.soff[j]] = v[j];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int MAXT, int MINB, bool BATCHED>
+__global__ void __launch_bounds__(MAXT, MINB) k_fused_pass(T* __restrict__ state,
+                                                         const __grid_constant__ PassParams<T> p,
+                                                         const __grid_constant__ BatchArgs<T> batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int kt = p.kt;
+  const int tsize = 1 << kt;
+  const int tstride = tile_stride(tsize);
+  T* const buf0 = reinterpret_cast<T*>(smem_raw);  // two tiles, tstride apart
+  int64_t* dep_hi = reinterpret_cast<int64_t*>(buf0 + 2 * tstride);
+  const int nhi = kt - kLowBits;
+  for (int h = threadIdx.x; h < (1 << nhi); h += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < nhi; b++)
+      if ((h >> b) & 1) o |= (int64_t)1 << p.tile_pos[kLowBits + b];
+    dep_hi[h] = o;
+  }
+  __syncthreads();
+  const int nthreads = blockDim.x;
+  auto issue_load = [&](T* buf, const T* st, int64_t base) {
+    for (int e = threadIdx.x; e < tsize; e += nthreads)
+      cp_async<sizeof(T)>(buf + smem_pos(e), st + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))));
+    cp_async_commit();
+  };
+  // items: (circuit, tile) for batched runs, tiles of the one state otherwise
+  const int64_t nitems = BATCHED ? p.ntiles * batch.ncirc : p.ntiles;
+  const int tshift = p.n - kt;  // ntiles = 2^tshift
+  auto item_state = [&](int64_t it) -> T* {
+    if constexpr (BATCHED) return batch.states[it >> tshift];
+    else return state;
+  };
+  auto item_tile = [&](int64_t it) -> int64_t { return BATCHED ? (it & (p.ntiles - 1)) : it; };
+  int64_t t = blockIdx.x;
+  if (t < nitems) issue_load(buf0, item_state(t), tile_origin(item_tile(t), p.tile_pos, kt));
+  int cur = 0;
+  for (; t < nitems; t += gridDim.x, cur ^= 1) {
+    T* tile = buf0 + cur * tstride;
+    T* const st = item_state(t);
+    const int64_t base = tile_origin(item_tile(t), p.tile_pos, kt);
+    const T* cbase;
+    if constexpr (BATCHED) cbase = batch.coef + (t >> tshift) * batch.coef_stride + p.coef_goff;
+    else cbase = p.coef;
+    const int64_t tn = t + gridDim.x;
+    if (tn < nitems) {
+      issue_load(buf0 + (cur ^ 1) * tstride, item_state(tn), tile_origin(item_tile(tn), p.tile_pos, kt));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    if constexpr (stored_as_double_pairs<T>::value) {
+      // the tile arrived as complex128 bytes: convert it to float pairs in place, once
+      // per pass (the final stores convert back)
+      for (int e = threadIdx.x; e < tsize; e += nthreads) cw_from_stored(tile + smem_pos(e));
       __syncthreads();
     }
+    tile_phases(p, tile, cbase, base, true);
     for (int e = threadIdx.x; e < tsize; e += nthreads)
       stg_stream(st + (base | dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1))), tile[smem_pos(e)]);
     __syncthreads();  // this buffer is refilled by the prefetch two tiles later
@@ -1541,6 +1554,7 @@ int sv_program_destroy(sv_program* prog) {
 namespace sv {
 
 constexpr int kBatchStreams = 4;
+constexpr int kPersistChunkBits = 2;  // persistent executor: up to 4 tiles of one circuit per ticket
 
 struct BatchGroup {
   sv_program* prog = nullptr;
@@ -1566,6 +1580,16 @@ struct sv_batch {
   cudaEvent_t ev_fork = nullptr, ev_join[sv::kBatchStreams] = {};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // executor: SV_BATCH_GRAPH (a launch per group and pass, four streams, one graph) or
+  // SV_BATCH_PERSISTENT (one cooperative launch); eager: the runs are not recorded
+  int executor = 0;
+  bool eager = false;
+  void* d_pparams = nullptr;           // persistent: every group's pass blocks
+  void* d_plaunch = nullptr;           // persistent: the (group, pass) queue
+  int* d_pcnt = nullptr;               // persistent: per-circuit tile counters, ticket, abort flag
+  int p_nl = 0, p_ncnt = 0, p_threads = 0;
+  int64_t p_ntickets = 0;
+  size_t p_smem = 0;
   // energies
   int nblocks = 0;
   void* d_blocks = nullptr;            // int2 (circuit, block index within circuit) per energy block
@@ -1645,6 +1669,171 @@ __global__ void k_tfim_finish(const double* partials, const int* nb, const int* 
   energy[c] = s + comp;
 }
 
+// ------------------------------------------------- persistent batched executor
+// One cooperative launch runs every pass of every group.  Work comes as tickets in
+// queue order -- round r holds every group's pass r, largest states first -- and a
+// ticket is a run of 2^cshift tiles of one circuit in one pass.  A ticket of pass
+// r > 0 waits until its circuit's pass r - 1 has finished all its tiles (per-circuit
+// tile counters, released with a fence, read with acquire loads).  Every ticket's
+// dependencies precede it in the queue and the blocks, all resident, take tickets in
+// order, so the earliest unfinished ticket can always proceed; a wait that exceeds its
+// time limit raises the abort flag for every block and leaves status 2.
+struct PLaunch {
+  int64_t first;          // first ticket of this (group, pass)
+  const void* params;     // the pass's PassParams block (device copy)
+  const void* states;     // the group's state pointer table
+  const void* coef;       // the group's coefficient blocks
+  int64_t coef_stride;
+  int32_t tshift;         // log2 tiles per circuit
+  int32_t cshift;         // log2 tiles per ticket
+  int32_t cnt;            // this pass's per-circuit counters (offset)
+  int32_t prev;           // the previous pass's counters (offset), -1 for a group's first pass
+};
+
+constexpr unsigned long long kPersistWaitNs = 2000000000ull;  // 2 s; a ticket takes microseconds
+
+__device__ __forceinline__ unsigned long long persist_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// loads that bypass L1 (the previous pass was written by other SMs during this launch)
+template <typename T> __device__ __forceinline__ T ld_l2(const T* p);
+template <> __device__ __forceinline__ c64 ld_l2<c64>(const c64* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return c64{v.x, v.y};
+}
+template <> __device__ __forceinline__ c128 ld_l2<c128>(const c128* p) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return c128{v.x, v.y};
+}
+template <> __device__ __forceinline__ cw ld_l2<cw>(const cw* p) {  // stored as complex128
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return cw(dw_from_double(v.x), dw_from_double(v.y));
+}
+// plain stores (the next pass may read them from L2)
+template <typename T> __device__ __forceinline__ void st_plain(T* p, T v) { *p = v; }
+template <> __device__ __forceinline__ void st_plain<cw>(cw* p, cw v) {
+  *reinterpret_cast<double2*>(p) = make_double2(dw_to_double(v.re), dw_to_double(v.im));
+}
+
+template <typename T, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_batch_persistent(const PLaunch* __restrict__ L, int nl,
+                                                               int64_t ntickets, unsigned long long* ticket,
+                                                               int* cnt, int* abort_flag, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_t;
+  __shared__ int s_l, s_go;
+  T* const tile = reinterpret_cast<T*>(smem_raw);
+  // the largest tile (2^kRB amplitudes per thread), then its outer-bit deposit table
+  int64_t* const dep_hi = reinterpret_cast<int64_t*>(smem_raw + sizeof(T) * (size_t)tile_stride(blockDim.x << kRB));
+  int cur_l = -1;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const long long t = (long long)atomicAdd(ticket, 1ull);
+      int go = t < ntickets && !*(volatile int*)abort_flag;
+      int l = 0;
+      if (go) {
+        // the last (group, pass) whose first ticket is <= t: a block's tickets increase,
+        // so the search starts at its previous one and gallops forward
+        int lo = cur_l < 0 ? 0 : cur_l, hi = lo + 1, step = 1;  // L[lo].first <= t
+        while (hi < nl && L[hi].first <= t) {
+          lo = hi;
+          hi += step;
+          step <<= 1;
+        }
+        if (hi > nl - 1) hi = nl - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (L[mid].first <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        l = lo;
+        const PLaunch& la = L[l];
+        if (la.prev >= 0) {
+          const int c = (int)(((t - la.first) << la.cshift) >> la.tshift);
+          const int need = 1 << la.tshift;
+          const unsigned long long t0 = persist_clock();
+          while (ld_acquire_gpu(cnt + la.prev + c) < need) {
+            if (*(volatile int*)abort_flag) {
+              go = 0;
+              break;
+            }
+            if (persist_clock() - t0 > kPersistWaitNs) {
+              atomicExch(abort_flag, 1);
+              atomicExch(status, 2);
+              go = 0;
+              break;
+            }
+            __nanosleep(128);
+          }
+        }
+      }
+      s_t = t;
+      s_l = l;
+      s_go = go;
+    }
+    __syncthreads();
+    if (!s_go) break;
+    const long long t = s_t;
+    const int l = s_l;
+    const PLaunch& la = L[l];
+    const PassParams<T>& p = *reinterpret_cast<const PassParams<T>*>(la.params);
+    const int kt = p.kt;
+    const int tsize = 1 << kt;
+    if (l != cur_l) {  // this pass's tile map
+      const int nhi = kt - kLowBits;
+      for (int h = threadIdx.x; h < (1 << nhi); h += blockDim.x) {
+        int64_t o = 0;
+        for (int b = 0; b < nhi; b++)
+          if ((h >> b) & 1) o |= (int64_t)1 << p.tile_pos[kLowBits + b];
+        dep_hi[h] = o;
+      }
+      cur_l = l;
+      __syncthreads();
+    }
+    const int64_t first_tile = (int64_t)(t - la.first) << la.cshift;
+    const int c = (int)(first_tile >> la.tshift);
+    T* const st = reinterpret_cast<T* const*>(la.states)[c];
+    const T* const cbase = reinterpret_cast<const T*>(la.coef) + (int64_t)c * la.coef_stride + p.coef_goff;
+    const bool active = (int)threadIdx.x < (tsize >> kRB);
+    auto gofs = [&](int e) { return dep_hi[e >> kLowBits] | (e & ((1 << kLowBits) - 1)); };
+    for (int k = 0; k < (1 << la.cshift); k++) {
+      const int64_t base = tile_origin((first_tile + k) & ((1ll << la.tshift) - 1), p.tile_pos, kt);
+      // element threadIdx.x + i * blockDim.x, i < 2^kRB: all of a thread's loads in flight
+      T r[1 << kRB];
+#pragma unroll
+      for (int i = 0; i < (1 << kRB); i++) {
+        const int e = threadIdx.x + i * blockDim.x;
+        if (e < tsize) r[i] = ld_l2(st + (base | gofs(e)));
+      }
+#pragma unroll
+      for (int i = 0; i < (1 << kRB); i++) {
+        const int e = threadIdx.x + i * blockDim.x;
+        if (e < tsize) tile[smem_pos(e)] = r[i];
+      }
+      __syncthreads();
+      tile_phases(p, tile, cbase, base, active);
+#pragma unroll
+      for (int i = 0; i < (1 << kRB); i++) {
+        const int e = threadIdx.x + i * blockDim.x;
+        if (e < tsize) st_plain(st + (base | gofs(e)), tile[smem_pos(e)]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {  // release: the block's stores before the count
+      __threadfence();
+      atomicAdd(cnt + la.cnt + c, 1 << la.cshift);
+    }
+  }
+}
+
 static bool same_structure(const std::vector<HostOp>& a, const std::vector<HostOp>& b) {
   if (a.size() != b.size()) return false;
   for (size_t i = 0; i < a.size(); i++) {
@@ -1702,8 +1891,111 @@ static int batch_build(sv_batch* b) {
   return SV_OK;
 }
 
+// the persistent executor's queue: every group's pass r for r = 0, 1, ..., groups in
+// their order (largest states first); pass blocks copied to the device once
+template <typename T>
+static int persist_build(Context* ctx, sv_batch* b) {
+  std::vector<PLaunch> ls;
+  std::vector<size_t> pofs;  // each group's first pass block in the device copy
+  size_t pbytes = 0;
+  int maxp = 0, ktmax = kRB + 1;
+  for (const BatchGroup& g : b->groups) {
+    for (const Segment& s : g.prog->segments)
+      if (!s.fused) return set_error(SV_ERR_UNSUPPORTED, "the persistent executor runs fused passes only");
+    pofs.push_back(pbytes);
+    pbytes += g.prog->passes.size();
+    maxp = std::max(maxp, (int)g.prog->segments.size());
+    ktmax = std::max(ktmax, g.prog->kt);
+  }
+  if (pbytes == 0) return set_error(SV_ERR_ARG, "the batch has no passes");
+  std::vector<unsigned char> blocks(pbytes);
+  for (size_t gi = 0; gi < b->groups.size(); gi++) {
+    const sv_program* prog = b->groups[gi].prog;
+    const std::vector<unsigned char>& src = b->dw ? prog->passes_dw : prog->passes;
+    memcpy(blocks.data() + pofs[gi], src.data(), src.size());
+  }
+  SV_TRY(check_cuda(cudaMalloc(&b->d_pparams, pbytes), "persistent pass blocks"));
+  SV_TRY(check_cuda(cudaMemcpy(b->d_pparams, blocks.data(), pbytes, cudaMemcpyHostToDevice), "pass block upload"));
+  std::vector<int> prev(b->groups.size(), -1);
+  int64_t tickets = 0;
+  int counters = 0;
+  for (int r = 0; r < maxp; r++)
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+      const BatchGroup& g = b->groups[gi];
+      const sv_program* prog = g.prog;
+      if (r >= (int)prog->segments.size()) continue;
+      PLaunch x;
+      memset(&x, 0, sizeof(x));
+      x.first = tickets;
+      x.params = (const char*)b->d_pparams + pofs[gi] + (size_t)prog->segments[r].pass * prog->pass_bytes;
+      x.states = g.d_states;
+      x.coef = b->dw ? g.d_coef_dw : g.d_coef;
+      x.coef_stride = (int64_t)prog->coef_total;
+      x.tshift = prog->nqubits - prog->kt;
+      x.cshift = std::min(x.tshift, kPersistChunkBits);
+      x.cnt = counters;
+      x.prev = prev[gi];
+      prev[gi] = counters;
+      counters += (int)g.circuits.size();
+      tickets += (int64_t)g.circuits.size() << (x.tshift - x.cshift);
+      ls.push_back(x);
+    }
+  SV_TRY(check_cuda(cudaMalloc(&b->d_plaunch, ls.size() * sizeof(PLaunch)), "persistent queue"));
+  SV_TRY(check_cuda(cudaMemcpy(b->d_plaunch, ls.data(), ls.size() * sizeof(PLaunch), cudaMemcpyHostToDevice),
+                    "queue upload"));
+  SV_TRY(check_cuda(cudaMalloc(&b->d_pcnt, sizeof(int) * (size_t)counters + 16), "persistent counters"));
+  b->p_nl = (int)ls.size();
+  b->p_ncnt = counters;
+  b->p_ntickets = tickets;
+  b->p_threads = 1 << (ktmax - kRB);
+  b->p_smem = sizeof(T) * (size_t)tile_stride(1 << ktmax) + sizeof(int64_t) * ((size_t)1 << (ktmax - kLowBits));
+  (void)ctx;
+  return SV_OK;
+}
+
+template <typename T, int MAXT, int MINB>
+static int persist_launch_variant(Context* ctx, sv_batch* b, cudaStream_t st) {
+  auto kern = k_batch_persistent<T, MAXT, MINB>;
+  SV_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->p_smem),
+                    "persistent executor smem attribute"));
+  int per_sm = 0;
+  SV_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, b->p_threads, b->p_smem),
+                    "persistent executor occupancy"));
+  if (per_sm < 1) return set_error(SV_ERR_ARG, "the persistent executor's tile does not fit on an SM");
+  int64_t grid = (int64_t)per_sm * ctx->num_sms;  // all blocks resident (cooperative launch)
+  if (grid > b->p_ntickets) grid = b->p_ntickets;
+  const PLaunch* dl = (const PLaunch*)b->d_plaunch;
+  int nl = b->p_nl;
+  int64_t nt = b->p_ntickets;
+  int* cnt = b->d_pcnt;
+  unsigned long long* ticket = (unsigned long long*)(cnt + b->p_ncnt + (b->p_ncnt & 1));  // 8-byte aligned
+  int* abort_flag = (int*)(ticket + 1);
+  int* status = ctx->device_status;
+  SV_TRY(check_cuda(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)b->p_ncnt + 16, st), "counter reset"));
+  void* args[] = {&dl, &nl, &nt, &ticket, &cnt, &abort_flag, &status};
+  SV_TRY(check_cuda(cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)grid), dim3(b->p_threads), args,
+                                                b->p_smem, st),
+                    "persistent executor launch"));
+  return SV_OK;
+}
+
+// |0...0> for every circuit, then the whole batch in one cooperative launch
+template <typename T>
+static int persist_launches(Context* ctx, sv_batch* b) {
+  cudaStream_t st = b->streams[0];
+  const size_t es = b->dtype == SV_C128 ? sizeof(c128) : sizeof(c64);
+  SV_TRY(check_cuda(cudaMemsetAsync(b->d_buf, 0, b->total * es, st), "batch zero"));
+  if (b->dtype == SV_C128) k_batch_ones<c128><<<grid_for(b->ncirc, 256), 256, 0, st>>>((c128* const*)b->d_ptrs, b->ncirc);
+  else k_batch_ones<c64><<<grid_for(b->ncirc, 256), 256, 0, st>>>((c64* const*)b->d_ptrs, b->ncirc);
+  SV_LAUNCH_CHECK("batch ones");
+  if constexpr (sizeof(T) >= 16) return persist_launch_variant<T, 256, 1>(ctx, b, st);
+  else if (b->p_threads <= 256) return persist_launch_variant<T, 256, 2>(ctx, b, st);
+  else return persist_launch_variant<T, 512, 1>(ctx, b, st);
+}
+
 template <typename T>
 static int batch_launches(Context* ctx, sv_batch* b) {
+  if (b->executor == SV_BATCH_PERSISTENT) return b->dw ? persist_launches<cw>(ctx, b) : persist_launches<T>(ctx, b);
   const size_t bytes = b->total * sizeof(T);
   SV_TRY(check_cuda(cudaMemsetAsync(b->d_buf, 0, bytes, b->streams[0]), "batch zero"));
   k_batch_ones<T><<<grid_for(b->ncirc, 256), 256, 0, b->streams[0]>>>((T* const*)b->d_ptrs, b->ncirc);
@@ -1760,6 +2052,9 @@ static int batch_launches(Context* ctx, sv_batch* b) {
 
 static void batch_free(sv_batch* b) {
   if (!b) return;
+  if (b->d_pparams) cudaFree(b->d_pparams);
+  if (b->d_plaunch) cudaFree(b->d_plaunch);
+  if (b->d_pcnt) cudaFree(b->d_pcnt);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   for (auto& g : b->groups) {
@@ -1895,6 +2190,36 @@ int sv_batch_create(sv_context* ctx, int dtype, int ncirc, const int32_t* nqubit
   return SV_OK;
 }
 
+int sv_batch_set_executor(sv_context* ctx, sv_batch* b, int executor) {
+  if (!ctx || !b) return set_error(SV_ERR_ARG, "null context or batch");
+  if (executor != SV_BATCH_GRAPH && executor != SV_BATCH_PERSISTENT)
+    return set_error(SV_ERR_ARG, "executor must be SV_BATCH_GRAPH or SV_BATCH_PERSISTENT");
+  SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
+  SV_TRY(check_cuda(cudaStreamSynchronize(b->streams[0]), "batch sync"));
+  if (executor == SV_BATCH_PERSISTENT && !b->d_plaunch) {
+    SV_TRY(ensure_device_status(ctx));
+    int rc = b->dw ? persist_build<cw>(ctx, b) : b->dtype == SV_C128 ? persist_build<c128>(ctx, b)
+                                                                     : persist_build<c64>(ctx, b);
+    if (rc != SV_OK) {
+      if (b->d_pparams) cudaFree(b->d_pparams);
+      if (b->d_plaunch) cudaFree(b->d_plaunch);
+      if (b->d_pcnt) cudaFree(b->d_pcnt);
+      b->d_pparams = b->d_plaunch = nullptr;
+      b->d_pcnt = nullptr;
+      return rc;
+    }
+  }
+  if (executor != b->executor) {  // record the new launches on the next run
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->eager = false;
+    b->executor = executor;
+  }
+  return SV_OK;
+}
+
 int sv_batch_specialize(sv_context* ctx, sv_batch* b) {
   if (!ctx || !b) return set_error(SV_ERR_ARG, "null context or batch");
   SV_TRY(check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"));
@@ -1916,8 +2241,11 @@ int sv_batch_run(sv_context* ctx, sv_batch* b) {
   SV_TRY(check_cuda(cudaEventRecord(ev, ctx->stream), "event"));
   SV_TRY(check_cuda(cudaStreamWaitEvent(b->streams[0], ev, 0), "wait"));
   int rc = SV_OK;
+  if (b->executor == SV_BATCH_PERSISTENT) ctx->status_pending = true;  // its waits are bounded
   if (b->exec) {
     rc = check_cuda(cudaGraphLaunch(b->exec, b->streams[0]), "graph launch");
+  } else if (b->eager) {
+    rc = b->dtype == SV_C128 ? batch_launches<c128>(ctx, b) : batch_launches<c64>(ctx, b);
   } else {
     // first run: eager (sets kernel attributes), then record the same launches as a graph
     rc = b->dtype == SV_C128 ? batch_launches<c128>(ctx, b) : batch_launches<c64>(ctx, b);
@@ -1933,6 +2261,16 @@ int sv_batch_run(sv_context* ctx, sv_batch* b) {
         rc = check_cuda(cudaGraphInstantiate(&b->exec, g, 0), "graph instantiate");
       } else if (g) {
         cudaGraphDestroy(g);
+      }
+      if (rc != SV_OK && b->executor == SV_BATCH_PERSISTENT) {
+        // a cooperative launch that cannot be recorded runs eagerly on later runs
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        (void)cudaGetLastError();
+        b->eager = true;
+        rc = SV_OK;
       }
     }
     // the eager run already produced the states; the graph is for later runs
@@ -1961,7 +2299,7 @@ int sv_batch_tfim_energy(sv_context* ctx, sv_batch* b, double h, double* energie
                                     ctx->stream), "energy copy"));
   SV_TRY(check_cuda(cudaStreamSynchronize(ctx->stream), "energy sync"));
   memcpy(energies, b->h_energy, b->ncirc * sizeof(double));
-  return SV_OK;
+  return take_device_status(ctx);  // a persistent run that gave up waiting reports here
 }
 
 int sv_batch_state(const sv_batch* b, int circuit, void** state, int* nqubits) {

@@ -103,3 +103,58 @@ def test_specialised_batch_of_random_circuits(backend):
     for i, c in enumerate(circs):
         want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits), fuse=False))
         np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("dt,tol", [("complex128", 1e-12), ("complex64", 2e-5)])
+def test_persistent_executor_matches_graph(backend, dt, tol):
+    """sv_batch_set_executor(SV_BATCH_PERSISTENT): the whole batch in one cooperative
+    launch (per-circuit pass ordering through device counters) gives the interpreting
+    graph executor's states and energies; circuits of 8 to 15 qubits mix tiles smaller
+    than the launch's largest; a second run (recorded or eager) repeats the first."""
+    specs = hea_batch(40, seed=23, nmin=8, nmax=15, lmin=2, lmax=6)
+    circs = [hea_circuit(n, L, p) for n, L, p in specs]
+    batch = BatchedCircuits(backend, circs, dt)
+    batch.run()
+    want = [backend.to_numpy(batch.state(i)).copy() for i in range(len(circs))]
+    e_graph = batch.tfim_energies(1.0)
+    batch.set_executor("persistent")
+    for _ in range(2):
+        batch.run()
+        e = batch.tfim_energies(1.0)
+        for i in range(len(circs)):
+            np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want[i], rtol=0, atol=tol)
+        np.testing.assert_allclose(e, e_graph, rtol=0, atol=1e-11 if dt == "complex128" else 1e-5)
+    for i, c in enumerate(circs[:6]):
+        ref = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits, dtype=dt), fuse=False))
+        np.testing.assert_allclose(backend.to_numpy(batch.state(i)), ref, rtol=0, atol=tol)
+    batch.set_executor("graph")
+    batch.run()
+    np.testing.assert_allclose(batch.tfim_energies(1.0), e_graph, rtol=0, atol=1e-12 if dt == "complex128" else 1e-6)
+    batch.close()
+
+
+def test_persistent_executor_random_circuits(backend):
+    """Many structures (every fusable gate family), complex128 in double-word and FP64
+    arithmetic, against the per-gate path."""
+    circs = [random_circuit(9 + (k % 4), 50, seed=500 + k % 5,
+                            families=["one", "one_p", "two_c", "two_p", "swap", "fsim", "u2q", "zc", "ccz", "toffoli"])
+             for k in range(12)]
+    for mode in ("double-word", "fp64"):
+        backend.ctx.set_c128_arithmetic(mode)
+        try:
+            batch = BatchedCircuits(backend, circs, "complex128")
+        finally:
+            backend.ctx.set_c128_arithmetic("double-word")
+        batch.set_executor("persistent").run()
+        batch.tfim_energies(1.0)  # synchronises and reports a timed-out wait
+        for i, c in enumerate(circs):
+            want = backend.to_numpy(backend.execute_circuit(c, backend.zero_state(c.nqubits), fuse=False))
+            np.testing.assert_allclose(backend.to_numpy(batch.state(i)), want, rtol=0, atol=1e-12)
+        batch.close()
+
+
+def test_executor_name_is_checked(backend):
+    batch = BatchedCircuits(backend, [hea_circuit(8, 2, np.zeros((2, 8, 2)))], "complex64")
+    with pytest.raises(ValueError):
+        batch.set_executor("threads")
+    batch.close()
