@@ -614,6 +614,12 @@ def _extra_workloads(torch, backend, stream, args):
             return e0.elapsed_time(e1) / reps
 
         ms_interp = timed_runs()  # interpreting pass kernel
+        # the whole batch in one cooperative launch (interpreting kernel), then back to
+        # the graph of per-group launches
+        bat.set_executor("persistent")
+        ms_persist = timed_runs()
+        e_persist = bat.tfim_energies(1.0)
+        bat.set_executor("graph")
         ms, spec_s = ms_interp, None
         # complex128 batches run the interpreting double-word kernel: compiling every
         # group's double-word passes takes minutes and measured no faster (3.87 against
@@ -628,7 +634,9 @@ def _extra_workloads(torch, backend, stream, args):
         st = bat.stats()
         vq[dt] = {"circuits_per_s": 4096 / (ms / 1000.0), "ms_per_batch": ms, "energy_ms":
                   1000 * (time.perf_counter() - t0), "plan_s": create_s, "specialise_s": spec_s,
-                  "interpreted_circuits_per_s": 4096 / (ms_interp / 1000.0), "stats": st,
+                  "interpreted_circuits_per_s": 4096 / (ms_interp / 1000.0),
+                  "persistent_single_launch_circuits_per_s": 4096 / (ms_persist / 1000.0),
+                  "persistent_max_abs_energy_diff": float(np.abs(e_persist - en).max()), "stats": st,
                   # every circuit's plan passes, each one read and one write of its state
                   "roofline": _frac(st["pass_bytes"], ms)}
         vq[dt]["energies_head"] = [float(v) for v in en[:3]]
