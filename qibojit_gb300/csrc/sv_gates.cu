@@ -179,6 +179,90 @@ __global__ void __launch_bounds__(kBlock) k_multi_reg(T* __restrict__ s, int64_t
   }
 }
 
+// ------------------------------------------ k targets on the lowest k bits, coalesced
+// Without controls and with the targets on bits 0..k-1 (any order), group gi is the
+// 2^k consecutive amplitudes from gi * 2^k: a thread reading its own group would touch
+// one 2^k-element run per lane, 2^k * sizeof(T) bytes apart.  Here a warp takes 32
+// consecutive groups, loads and stores them coalesced (lane + 32 j) and regroups them
+// in its own shared-memory slice (one padding slot every 16 elements, every 8 for
+// 16-byte elements, so neither access pattern conflicts on banks).
+template <typename T, int K>
+__global__ void __launch_bounds__(kBlock) k_multi_low(T* __restrict__ s, int64_t nchunks,
+                                                      Mat<T, (1 << (2 * K))> g, const __grid_constant__ Strides st) {
+  constexpr int N = 1 << K;
+  constexpr int CH = 32 * N;                       // amplitudes per warp
+  constexpr int PS = sizeof(T) >= 16 ? 3 : 4;      // padding: one slot per 2^PS elements
+  constexpr int PADDED = CH + (CH >> PS);
+  __shared__ T buf[kBlock / 32][PADDED];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t chunk = (int64_t)blockIdx.x * (kBlock / 32) + warp;
+  if (chunk >= nchunks) return;  // whole warps only: the kernel synchronises warps, not blocks
+  T* const base = s + chunk * CH;
+  T* const b = buf[warp];
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    const int e = lane + 32 * j;
+    b[e + (e >> PS)] = ldg_stream(base + e);
+  }
+  __syncwarp();
+  int off[N];
+  T in[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    int o = 0;
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if ((i >> u) & 1) o += (int)st.ts[u];
+    const int e = lane * N + o;
+    off[i] = e + (e >> PS);
+    in[i] = b[off[i]];
+  }
+  // every lane rewrites only the slots it read
+#pragma unroll
+  for (int r = 0; r < N; r++) {
+    T acc = tmul(g.g[r * N], in[0]);
+#pragma unroll
+    for (int c = 1; c < N; c++) acc = tfma(g.g[r * N + c], in[c], acc);
+    b[off[r]] = acc;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    const int e = lane + 32 * j;
+    stg_stream(base + e, b[e + (e >> PS)]);
+  }
+}
+
+// ------------------------------------------ k targets, complex128 in double-word arithmetic
+// As k_multi_reg, each output a double-word dot product of a matrix row (split into
+// float pairs on the host) with the group's 2^K amplitudes (cdw_dot, sv_dw.cuh).
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_multi_dw(c128* __restrict__ s, int64_t ngroups,
+                                                     Mat<cdw, (1 << (2 * K))> g, const __grid_constant__ BitList q,
+                                                     const __grid_constant__ Strides st) {
+  constexpr int N = 1 << K;
+  const int64_t gi = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (gi >= ngroups) return;
+  const int64_t i0 = insert_ones(gi, q) - st.zero_off;
+  int64_t off[N];
+  double2 raw[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    int64_t o = 0;
+#pragma unroll
+    for (int u = 0; u < K; u++)
+      if ((i >> u) & 1) o += st.ts[u];
+    off[i] = o;
+    raw[i] = __ldcs(reinterpret_cast<const double2*>(s + i0 + o));
+  }
+  cdw in[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) in[i] = cdw_load(raw[i]);
+#pragma unroll
+  for (int r = 0; r < N; r++)
+    __stcs(reinterpret_cast<double2*>(s + i0 + off[r]), cdw_store(cdw_dot<N>(&g.g[r * N], in)));
+}
+
 // ------------------------------------------------- k targets, shared-memory groups
 // A block stages NG groups (NG * 2^k amplitudes, <= 32 KB) in shared memory, laid
 // out [row][group] so that consecutive threads read consecutive groups, then every
@@ -498,6 +582,26 @@ static int launch_multi_reg(Context* ctx, void* state, int64_t ngroups, const vo
   return SV_OK;
 }
 
+template <typename T, int K>
+static int launch_multi_low(Context* ctx, void* state, int64_t ngroups, const void* gate, const Strides& st) {
+  Mat<T, (1 << (2 * K))> g;
+  memcpy(g.g, gate, sizeof(g.g));
+  const int64_t nchunks = ngroups / 32;  // 32 groups per warp
+  k_multi_low<T, K><<<grid_for(nchunks, kBlock / 32), kBlock, 0, ctx->stream>>>((T*)state, nchunks, g, st);
+  SV_LAUNCH_CHECK("multi-qubit (low targets) kernel launch");
+  return SV_OK;
+}
+
+template <int K>
+static int launch_multi_dw(Context* ctx, void* state, int64_t ngroups, const void* gate, const BitList& q,
+                           const Strides& st) {
+  Mat<cdw, (1 << (2 * K))> g;
+  split_operand(g, (const c128*)gate, 1 << (2 * K));
+  k_multi_dw<K><<<grid_for(ngroups, kBlock), kBlock, 0, ctx->stream>>>((c128*)state, ngroups, g, q, st);
+  SV_LAUNCH_CHECK("multi-qubit double-word kernel launch");
+  return SV_OK;
+}
+
 template <typename T>
 static int multi_qubit_typed(Context* ctx, void* state, int nqubits, const void* gate,
                              const int32_t* targets, int k, const BitList& q) {
@@ -508,6 +612,18 @@ static int multi_qubit_typed(Context* ctx, void* state, int nqubits, const void*
     st.zero_off += st.ts[u];
   }
   const int64_t ngroups = (int64_t)1 << (nqubits - q.n);
+  if constexpr (std::is_same<T, c128>::value) {
+    // complex128 in double-word arithmetic unless the context asks for FP64
+    if (!ctx->c128_fp64 && k == 3) return launch_multi_dw<3>(ctx, state, ngroups, gate, q, st);
+    if (!ctx->c128_fp64 && k == 4) return launch_multi_dw<4>(ctx, state, ngroups, gate, q, st);
+  }
+  // no controls, targets on bits 0..k-1 in any order, at least one warp of groups
+  int64_t low_mask = 0;
+  for (int u = 0; u < k; u++) low_mask |= st.ts[u];
+  if (q.n == k && low_mask == ((int64_t)1 << k) - 1 && ngroups >= 32) {
+    if (k == 3) return launch_multi_low<T, 3>(ctx, state, ngroups, gate, st);
+    if (k == 4 && sizeof(T) <= 8) return launch_multi_low<T, 4>(ctx, state, ngroups, gate, st);
+  }
   switch (k) {
     case 1: return launch_multi_reg<T, 1>(ctx, state, ngroups, gate, q, st);
     case 2: return launch_multi_reg<T, 2>(ctx, state, ngroups, gate, q, st);

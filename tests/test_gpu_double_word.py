@@ -87,6 +87,28 @@ def test_two_target_double_word_vs_oracle_and_fp64(backend, n, t1, t2, controls,
         assert np.all(np.abs(dwr - want) <= 1.2e-13 * _row_scale(oracle, state, gate) + 1e-28)
 
 
+MULTI = [(12, [0, 5, 11], []), (12, [9, 10, 11], []), (14, [3, 7, 1, 12], []), (16, [15, 12, 13, 14], [2]),
+         (14, [6, 0, 13], [4, 9])]
+
+
+@pytest.mark.parametrize("n,targets,controls", MULTI)
+def test_multi_target_double_word_vs_oracle_and_fp64(backend, n, targets, controls):
+    """3 and 4 targets (any bits, with and without controls) in double-word arithmetic,
+    against the oracle and the FP64 kernels, on states spanning many magnitudes."""
+    ob = O.OracleBackend()
+    q = ob.qubits_tensor(n, targets, controls)
+    gate = random_unitary(2 ** len(targets), n + len(targets))
+    oracle = lambda x, g: ob._multi_qubit_base(x.copy(), n, targets, g, q)  # noqa: E731
+    for state in (random_state(n, 7 + n), _wide_state(n, 8 + n)):
+        fn = lambda s: backend._multi_qubit_base(s, n, targets, gate, q)  # noqa: E731
+        dwr = _run(backend, "double-word", state, fn)
+        f64 = _run(backend, "fp64", state, fn)
+        want = oracle(state, gate)
+        np.testing.assert_allclose(dwr, want, rtol=0, atol=PARITY_ATOL["complex128"])
+        np.testing.assert_allclose(dwr, f64, rtol=0, atol=1e-13)
+        assert np.all(np.abs(dwr - want) <= 1.2e-13 * _row_scale(oracle, state, gate) + 1e-28)
+
+
 def test_double_word_circuit_depth(backend):
     """A 300-gate circuit of dense one- and two-target gates at n=18, gate by gate in
     double-word arithmetic, against the oracle: the per-gate errors stay far below the

@@ -309,6 +309,23 @@ def test_apply_multiqubit_gate_large(backend, nqubits, targets, controls, dtype)
     np.testing.assert_allclose(got, want, rtol=0, atol=PARITY_ATOL[dtype] * rank)
 
 
+@pytest.mark.parametrize(("nqubits", "targets", "controls"),
+                         [(12, [9, 10, 11], []), (12, [11, 10, 9], []), (20, [16, 17, 18, 19], []),
+                          (20, [19, 17, 16, 18], []), (8, [4, 5, 6, 7], []), (9, [6, 7, 8], [0]),
+                          (20, [18, 19, 16, 17], [3])])
+def test_multi_target_gate_on_lowest_bits(backend, nqubits, targets, controls, dtype):
+    """3 and 4 targets on the lowest bits without controls (any target order) take the
+    coalesced warp-regrouping kernel once there is at least one warp of groups; with
+    fewer groups or with controls the per-thread kernel runs.  Unitary operands, so the
+    bar is unscaled."""
+    state = random_state(nqubits, 31, dtype)
+    matrix = random_unitary(2 ** len(targets), 32).astype(dtype)
+    q = O.OracleBackend.qubits_tensor(nqubits, targets, controls)
+    got = _run(backend, lambda s: backend._multi_qubit_base(s, nqubits, targets, matrix, q), state)
+    want = O.OracleBackend()._multi_qubit_base(state.copy(), nqubits, targets, matrix, q)
+    np.testing.assert_allclose(got, want, rtol=0, atol=PARITY_ATOL[dtype])
+
+
 @pytest.mark.parametrize("use_qubits", [False, True])
 @pytest.mark.parametrize(("nqubits", "targets"), [(5, [2, 3, 4]), (4, [2, 0, 1])])
 def test_apply_multi_qubit_base(backend, nqubits, targets, use_qubits, dtype):
