@@ -522,7 +522,7 @@ def _c128_gate_variants(torch, backend, stream, n):
     """complex128 per-gate passes at n=30: double-word arithmetic on the FP32 pipe
     against FP64 instructions."""
     s = backend.zero_state(n, dtype="complex128")
-    u2, u4, u8, u16 = _unitary(2, 1), _unitary(4, 2), _unitary(8, 3), _unitary(16, 4)
+    u2, u4, u8, u16, u32 = _unitary(2, 1), _unitary(4, 2), _unitary(8, 3), _unitary(16, 4), _unitary(32, 5)
     cases = {
         "u3_target0": (lambda: backend._one_qubit_base(s, n, 0, "apply_gate", u2, None), 32 << n),
         "u3_target29": (lambda: backend._one_qubit_base(s, n, n - 1, "apply_gate", u2, None), 32 << n),
@@ -531,6 +531,7 @@ def _c128_gate_variants(torch, backend, stream, n):
         "two_target_3_17": (lambda: backend._two_qubit_base(s, n, 3, 17, "apply_two_qubit_gate", u4, None), 32 << n),
         "three_target_0_1_2": (lambda: backend._multi_qubit_base(s, n, [0, 1, 2], u8, None), 32 << n),
         "four_target_0_1_2_3": (lambda: backend._multi_qubit_base(s, n, [0, 1, 2, 3], u16, None), 32 << n),
+        "five_target_0_to_4": (lambda: backend._multi_qubit_base(s, n, [0, 1, 2, 3, 4], u32, None), 32 << n),
     }
     out = {}
     for name, (fn, nbytes) in cases.items():

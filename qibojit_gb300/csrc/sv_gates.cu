@@ -305,6 +305,55 @@ __global__ void __launch_bounds__(kBlock) k_multi_smem(T* __restrict__ s, int64_
   }
 }
 
+// k_multi_smem for complex128 in double-word arithmetic: groups staged as float pairs,
+// each output a double-word dot product with a matrix row split on the host
+__device__ __forceinline__ cdw ldg_cdw(const cdw* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  return cdw(dw{v.x, v.y}, dw{v.z, v.w});
+}
+
+__global__ void __launch_bounds__(kBlock) k_multi_smem_dw(c128* __restrict__ s, int64_t ngroups, int k,
+                                                          const cdw* __restrict__ gmat,
+                                                          const __grid_constant__ BitList q,
+                                                          const __grid_constant__ Strides st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cdw* buf = reinterpret_cast<cdw*>(smem_raw);
+  const int N = 1 << k;
+  const int NG = (int)(kSmemBytes / sizeof(cdw)) / N;  // groups per block (>= 1)
+  const int64_t g0 = (int64_t)blockIdx.x * NG;
+  const int total = NG * N;
+  for (int e = threadIdx.x; e < total; e += kBlock) {
+    const int i = e / NG, gg = e - i * NG;
+    const int64_t gi = g0 + gg;
+    if (gi < ngroups) {
+      int64_t o = 0;
+      for (int u = 0; u < k; u++)
+        if ((i >> u) & 1) o += st.ts[u];
+      buf[e] = cdw_load(__ldcs(reinterpret_cast<const double2*>(s + insert_ones(gi, q) - st.zero_off + o)));
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < total; e += kBlock) {
+    const int r = e / NG, gg = e - r * NG;
+    const int64_t gi = g0 + gg;
+    if (gi >= ngroups) continue;
+    const cdw* row = gmat + (size_t)r * N;
+    dwacc re{0.0f, 0.0f}, im{0.0f, 0.0f};
+    for (int c = 0; c < N; c++) {
+      const cdw m = ldg_cdw(row + c), v = buf[c * NG + gg];
+      dw_fma(re, m.re, v.re);
+      dw_fma(re, dw_neg(m.im), v.im);
+      dw_fma(im, m.re, v.im);
+      dw_fma(im, m.im, v.re);
+    }
+    int64_t o = 0;
+    for (int u = 0; u < k; u++)
+      if ((r >> u) & 1) o += st.ts[u];
+    __stcs(reinterpret_cast<double2*>(s + insert_ones(gi, q) - st.zero_off + o),
+           cdw_store(cdw(dwacc_result(re), dwacc_result(im))));
+  }
+}
+
 // ------------------------------------------------- complex128 in double-word arithmetic
 // The same index maps and load/store pattern as k_one_qubit / k_two_qubit; every
 // amplitude is converted to a (hi, lo) float pair on load and back on store, and each
@@ -616,6 +665,28 @@ static int multi_qubit_typed(Context* ctx, void* state, int nqubits, const void*
     // complex128 in double-word arithmetic unless the context asks for FP64
     if (!ctx->c128_fp64 && k == 3) return launch_multi_dw<3>(ctx, state, ngroups, gate, q, st);
     if (!ctx->c128_fp64 && k == 4) return launch_multi_dw<4>(ctx, state, ngroups, gate, q, st);
+    if (!ctx->c128_fp64 && k >= 5) {
+      const int n2 = 1 << (2 * k);
+      std::vector<cdw> split(n2);
+      const c128* m = (const c128*)gate;
+      for (int i = 0; i < n2; i++) {
+        sv_dw_split_host(m[i].re, &split[i].re.h, &split[i].re.l);
+        sv_dw_split_host(m[i].im, &split[i].im.h, &split[i].im.l);
+      }
+      const size_t mbytes = sizeof(cdw) * (size_t)n2;
+      SV_TRY(ensure_operand(ctx, mbytes));
+      // from pageable memory the copy is staged before the call returns, so the
+      // temporary may go out of scope
+      SV_TRY(check_cuda(cudaMemcpyAsync(ctx->operand, split.data(), mbytes, cudaMemcpyHostToDevice, ctx->stream),
+                        "gate operand upload"));
+      const int NG = (int)(kSmemBytes / sizeof(cdw)) >> k;
+      if (NG < 1) return set_error(SV_ERR_ARG, "%d targets exceed the shared-memory group size", k);
+      const int64_t nblocks = (ngroups + NG - 1) / NG;
+      k_multi_smem_dw<<<(unsigned)nblocks, kBlock, kSmemBytes, ctx->stream>>>((c128*)state, ngroups, k,
+                                                                              (const cdw*)ctx->operand, q, st);
+      SV_LAUNCH_CHECK("multi-qubit double-word (shared) kernel launch");
+      return SV_OK;
+    }
   }
   // no controls, targets on bits 0..k-1 in any order, at least one warp of groups
   int64_t low_mask = 0;

@@ -88,12 +88,13 @@ def test_two_target_double_word_vs_oracle_and_fp64(backend, n, t1, t2, controls,
 
 
 MULTI = [(12, [0, 5, 11], []), (12, [9, 10, 11], []), (14, [3, 7, 1, 12], []), (16, [15, 12, 13, 14], [2]),
-         (14, [6, 0, 13], [4, 9])]
+         (14, [6, 0, 13], [4, 9]), (13, [0, 2, 4, 6, 8], []), (14, [13, 12, 11, 10, 9, 8], [1]),
+         (12, [5, 1, 9, 3, 11, 7, 0], [])]
 
 
 @pytest.mark.parametrize("n,targets,controls", MULTI)
 def test_multi_target_double_word_vs_oracle_and_fp64(backend, n, targets, controls):
-    """3 and 4 targets (any bits, with and without controls) in double-word arithmetic,
+    """3 to 7 targets (any bits, with and without controls) in double-word arithmetic,
     against the oracle and the FP64 kernels, on states spanning many magnitudes."""
     ob = O.OracleBackend()
     q = ob.qubits_tensor(n, targets, controls)
