@@ -244,23 +244,24 @@ __global__ void __launch_bounds__(kBlock) k_multi_dw(c128* __restrict__ s, int64
   const int64_t gi = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   if (gi >= ngroups) return;
   const int64_t i0 = insert_ones(gi, q) - st.zero_off;
-  int64_t off[N];
-  double2 raw[N];
-#pragma unroll
-  for (int i = 0; i < N; i++) {
+  auto offset = [&](int i) {
     int64_t o = 0;
 #pragma unroll
     for (int u = 0; u < K; u++)
       if ((i >> u) & 1) o += st.ts[u];
-    off[i] = o;
-    raw[i] = __ldcs(reinterpret_cast<const double2*>(s + i0 + o));
-  }
+    return o;
+  };
+  double2 raw[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) raw[i] = __ldcs(reinterpret_cast<const double2*>(s + i0 + offset(i)));
   cdw in[N];
 #pragma unroll
   for (int i = 0; i < N; i++) in[i] = cdw_load(raw[i]);
-#pragma unroll
+  // one row per iteration, not unrolled: N unrolled double-word rows overflow the
+  // instruction cache (the matrix row is read from the parameters at a run-time offset)
+#pragma unroll 1
   for (int r = 0; r < N; r++)
-    __stcs(reinterpret_cast<double2*>(s + i0 + off[r]), cdw_store(cdw_dot<N>(&g.g[r * N], in)));
+    __stcs(reinterpret_cast<double2*>(s + i0 + offset(r)), cdw_store(cdw_dot<N>(&g.g[r * N], in)));
 }
 
 // ------------------------------------------------- k targets, shared-memory groups
