@@ -762,7 +762,8 @@ def precision_report(backend, n: int, depth: int) -> dict:
     stream = torch.cuda.current_stream()
     out = {}
     states = {}
-    for dt, spec in (("complex64", True), ("complex128", True)):
+    # complex128 on the interpreting kernel: its double-word passes outrun the compiled ones
+    for dt, spec in (("complex64", True), ("complex128", False)):
         t0 = time.perf_counter()
         prog = backend.compile(circ, dt, specialize=spec)
         plan_s = time.perf_counter() - t0
