@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "sv_plan.cuh"
+#include "sv_persist_queue.h"
 
 namespace sv {
 
@@ -1562,7 +1563,6 @@ int sv_program_destroy(sv_program* prog) {
 namespace sv {
 
 constexpr int kBatchStreams = 4;
-constexpr int kPersistChunkBits = 2;  // persistent executor: up to 4 tiles of one circuit per ticket
 
 struct BatchGroup {
   sv_program* prog = nullptr;
@@ -1899,20 +1899,20 @@ static int batch_build(sv_batch* b) {
   return SV_OK;
 }
 
-// the persistent executor's queue: every group's pass r for r = 0, 1, ..., groups in
-// their order (largest states first); pass blocks copied to the device once
+// the persistent executor's queue (persist_queue, sv_persist_queue.h) with device
+// pointers: pass blocks copied to the device once, the groups' state tables and
+// coefficient blocks
 template <typename T>
 static int persist_build(Context* ctx, sv_batch* b) {
   std::vector<PLaunch> ls;
   std::vector<size_t> pofs;  // each group's first pass block in the device copy
   size_t pbytes = 0;
-  int maxp = 0, ktmax = kRB + 1;
+  int ktmax = kRB + 1;
   for (const BatchGroup& g : b->groups) {
     for (const Segment& s : g.prog->segments)
       if (!s.fused) return set_error(SV_ERR_UNSUPPORTED, "the persistent executor runs fused passes only");
     pofs.push_back(pbytes);
     pbytes += g.prog->passes.size();
-    maxp = std::max(maxp, (int)g.prog->segments.size());
     ktmax = std::max(ktmax, g.prog->kt);
   }
   if (pbytes == 0) return set_error(SV_ERR_ARG, "the batch has no passes");
@@ -1924,30 +1924,29 @@ static int persist_build(Context* ctx, sv_batch* b) {
   }
   SV_TRY(check_cuda(cudaMalloc(&b->d_pparams, pbytes), "persistent pass blocks"));
   SV_TRY(check_cuda(cudaMemcpy(b->d_pparams, blocks.data(), pbytes, cudaMemcpyHostToDevice), "pass block upload"));
-  std::vector<int> prev(b->groups.size(), -1);
-  int64_t tickets = 0;
+  std::vector<PersistGroup> shape;
+  for (const BatchGroup& g : b->groups)
+    shape.push_back({(int)g.prog->segments.size(), (int)g.circuits.size(), g.prog->nqubits - g.prog->kt});
   int counters = 0;
-  for (int r = 0; r < maxp; r++)
-    for (size_t gi = 0; gi < b->groups.size(); gi++) {
-      const BatchGroup& g = b->groups[gi];
-      const sv_program* prog = g.prog;
-      if (r >= (int)prog->segments.size()) continue;
-      PLaunch x;
-      memset(&x, 0, sizeof(x));
-      x.first = tickets;
-      x.params = (const char*)b->d_pparams + pofs[gi] + (size_t)prog->segments[r].pass * prog->pass_bytes;
-      x.states = g.d_states;
-      x.coef = b->dw ? g.d_coef_dw : g.d_coef;
-      x.coef_stride = (int64_t)prog->coef_total;
-      x.tshift = prog->nqubits - prog->kt;
-      x.cshift = std::min(x.tshift, kPersistChunkBits);
-      x.cnt = counters;
-      x.prev = prev[gi];
-      prev[gi] = counters;
-      counters += (int)g.circuits.size();
-      tickets += (int64_t)g.circuits.size() << (x.tshift - x.cshift);
-      ls.push_back(x);
-    }
+  const std::vector<PersistEntry> queue = persist_queue(shape, &counters);
+  int64_t tickets = 0;
+  for (const PersistEntry& e : queue) {
+    const BatchGroup& g = b->groups[e.group];
+    const sv_program* prog = g.prog;
+    PLaunch x;
+    memset(&x, 0, sizeof(x));
+    x.first = e.first;
+    x.params = (const char*)b->d_pparams + pofs[e.group] + (size_t)prog->segments[e.pass].pass * prog->pass_bytes;
+    x.states = g.d_states;
+    x.coef = b->dw ? g.d_coef_dw : g.d_coef;
+    x.coef_stride = (int64_t)prog->coef_total;
+    x.tshift = e.tshift;
+    x.cshift = e.cshift;
+    x.cnt = e.cnt;
+    x.prev = e.prev;
+    tickets = e.first + e.ntickets;
+    ls.push_back(x);
+  }
   SV_TRY(check_cuda(cudaMalloc(&b->d_plaunch, ls.size() * sizeof(PLaunch)), "persistent queue"));
   SV_TRY(check_cuda(cudaMemcpy(b->d_plaunch, ls.data(), ls.size() * sizeof(PLaunch), cudaMemcpyHostToDevice),
                     "queue upload"));

@@ -115,3 +115,66 @@ def test_noalloc_grid_rule(tmp_path):
         if s <= 511:
             assert fits
     assert any(line.split()[3] == "0" for line in out if line and line.split()[0] == "512")
+
+
+def test_persistent_queue_order(tmp_path):
+    """The persistent batch executor's queue (csrc/sv_persist_queue.h), compiled with the
+    host compiler, on random group shapes: tickets are contiguous, counters disjoint,
+    every group's passes appear in order with each pass waiting on its predecessor's
+    counters, all of whose tickets precede it (so a single worker taking tickets in
+    order never waits on unfinished work: the property the kernel's bounded waits rely
+    on), and a circuit's tickets of one pass cover exactly its 2^tshift tiles."""
+    import random
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    src = tmp_path / "queue.cpp"
+    src.write_text(
+        '#include <stdio.h>\n#include "sv_persist_queue.h"\n'
+        "int main() {\n"
+        "  int ng;\n"
+        "  while (scanf(\"%d\", &ng) == 1) {\n"
+        "    std::vector<sv::PersistGroup> g(ng);\n"
+        "    for (auto& x : g) scanf(\"%d %d %d\", &x.npasses, &x.ncirc, &x.tshift);\n"
+        "    int nc = 0;\n"
+        "    auto q = sv::persist_queue(g, &nc);\n"
+        "    printf(\"%d %zu\\n\", nc, q.size());\n"
+        "    for (auto& e : q) printf(\"%d %d %lld %lld %d %d %d %d\\n\", e.group, e.pass, (long long)e.first,\n"
+        "                            (long long)e.ntickets, e.tshift, e.cshift, e.cnt, e.prev);\n"
+        "  }\n  return 0;\n}\n")
+    exe = tmp_path / "queue"
+    subprocess.run([cxx, "-std=c++17", "-I", os.path.join(ROOT, "qibojit_gb300", "csrc"), str(src), "-o", str(exe)],
+                   check=True)
+    rng = random.Random(3)
+    cases = [[(3, 2, 0)], [(1, 5, 4), (4, 3, 1), (2, 7, 9)]]
+    for _ in range(40):
+        cases.append([(rng.randint(1, 12), rng.randint(1, 300), rng.randint(0, 10)) for _ in range(rng.randint(1, 30))])
+    text = "".join(f"{len(c)} " + " ".join(f"{p} {n} {t}" for p, n, t in c) + "\n" for c in cases)
+    lines = subprocess.run([str(exe)], input=text, check=True, capture_output=True, text=True).stdout.split("\n")
+    pos = 0
+    for case in cases:
+        ncounters, nentries = (int(v) for v in lines[pos].split())
+        entries = [tuple(int(v) for v in lines[pos + 1 + i].split()) for i in range(nentries)]
+        pos += 1 + nentries
+        assert nentries == sum(p for p, _, _ in case)
+        nxt, used, seen = 0, set(), {}
+        for group, pss, first, nt, tshift, cshift, cnt, prev in entries:
+            npasses, ncirc, gt = case[group]
+            assert first == nxt and nt == ncirc << (tshift - cshift)
+            assert tshift == gt and cshift == min(tshift, 2)
+            assert (nt // ncirc) << cshift == 1 << tshift  # a circuit's tiles of this pass
+            nxt = first + nt
+            span = set(range(cnt, cnt + ncirc))
+            assert not (span & used)
+            used |= span
+            if pss == 0:
+                assert prev == -1
+            else:
+                before = seen[(group, pss - 1)]
+                assert prev == before[0] and before[1] <= first  # predecessor entirely earlier
+            seen[(group, pss)] = (cnt, first + nt)
+        assert len(used) == ncounters
+        for gi, (npasses, _, _) in enumerate(case):
+            assert all((gi, r) in seen for r in range(npasses))
