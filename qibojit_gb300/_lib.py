@@ -159,6 +159,7 @@ class Context:
         self._h = h
         self.lib = lib
         self.device = device
+        self.c128_arithmetic = "double-word"
         if stream:
             check(lib.sv_context_set_stream(h, _vp(stream)), "sv_context_set_stream")
 
@@ -173,11 +174,12 @@ class Context:
         check(self.lib.sv_sync(self._h), "sv_sync")
 
     def set_c128_arithmetic(self, mode: str) -> None:
-        """'double-word' (FP32 pipe, default) or 'fp64' for the complex128 per-gate kernels."""
+        """'double-word' (FP32 pipe, default) or 'fp64' for the complex128 kernels and passes."""
         codes = {"double-word": 0, "fp64": 1}
         if mode not in codes:
             raise ValueError(f"complex128 arithmetic must be one of {sorted(codes)}")
         check(self.lib.sv_context_set_c128_arithmetic(self._h, codes[mode]), "sv_context_set_c128_arithmetic")
+        self.c128_arithmetic = mode
 
     def set_dense_mode(self, mode: str) -> None:
         """'auto' (tensor cores for complex64 gates with 4..6 targets), 'simt' or 'tensor'."""

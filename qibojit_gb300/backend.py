@@ -620,13 +620,16 @@ class GB300Backend(_QiboBackend):
         content (every gate's class, qubits and parameter values), so a different or
         edited circuit never reuses a stale plan: a program that has run
         ``specialize_after`` times (counting the runs about to be made) is re-planned on
-        the larger tile and its passes specialised."""
+        the larger tile and its passes specialised (complex128 only in FP64 arithmetic)."""
         key = (_circuit_fingerprint(circuit), circuit.nqubits, dtype, bool(density_matrix))
         prog = self._programs.get(key)
         if prog is None:
             prog = self.compile(circuit, dtype, density_matrix=density_matrix)
             self._programs = {key: prog}
-        if (not prog.specialized and self.specialize_after is not None
+        # complex128 passes in double-word arithmetic run faster on the interpreting kernel
+        # (compiled double-word passes stall on instruction fetch): they stay interpreted
+        compiled_pays = dtype != "complex128" or getattr(self.ctx, "c128_arithmetic", "double-word") == "fp64"
+        if (compiled_pays and not prog.specialized and self.specialize_after is not None
                 and prog.runs + upcoming_runs - 1 >= self.specialize_after):
             runs = prog.runs
             prog = self.compile(circuit, dtype, specialize=True, density_matrix=density_matrix)

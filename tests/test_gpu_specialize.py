@@ -74,13 +74,22 @@ def test_execute_circuit_specialises_repeated_programs(backend):
     prog = backend._programs[key]
     assert prog.specialized and prog.stats()["tile_bits"] == 13
     np.testing.assert_allclose(again, first, rtol=0, atol=PARITY_ATOL["complex64"])
-    # complex128 programs too, on the default tile
+    # complex128 programs stay interpreted in double-word arithmetic (compiled double-word
+    # passes are slower) and are specialised in FP64 arithmetic
     y = random_state(n, 23)
     first128 = backend.to_numpy(backend.execute_circuit(circ, y))
     for _ in range(backend.specialize_after):
         again128 = backend.to_numpy(backend.execute_circuit(circ, y))
-    assert backend._programs[next(iter(backend._programs))].specialized
+    assert not backend._programs[next(iter(backend._programs))].specialized
     np.testing.assert_allclose(again128, first128, rtol=0, atol=1e-13)
+    backend.ctx.set_c128_arithmetic("fp64")
+    try:
+        for _ in range(backend.specialize_after):
+            f64 = backend.to_numpy(backend.execute_circuit(circ, y))
+        assert backend._programs[next(iter(backend._programs))].specialized
+        np.testing.assert_allclose(f64, first128, rtol=0, atol=1e-13)
+    finally:
+        backend.ctx.set_c128_arithmetic("double-word")
 
 
 @pytest.mark.parametrize("dt", ["complex64", "complex128"])
