@@ -207,7 +207,8 @@ def test_fused_density_circuit_matches_gate_by_gate(backend, n, ngates, seed, dt
         got = backend.to_numpy(backend.execute_circuit(circ, rho.copy()))
         np.testing.assert_allclose(got, want, atol=10 * ATOL[dtype])
     prog = next(iter(backend._programs.values()))
-    assert prog.nqubits == 2 * n and prog.specialized
+    # complex128 programs stay interpreted in double-word arithmetic (faster than compiled)
+    assert prog.nqubits == 2 * n and prog.specialized == (dtype == "complex64")
     backend.set_dtype("complex128")
 
 
