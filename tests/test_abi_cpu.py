@@ -69,6 +69,14 @@ def test_null_context_is_rejected(lib):
         _lib.check(rc)
 
 
+def test_null_handles_are_rejected_by_batch_and_adjoint_entry_points(lib):
+    """The batch executor switch and the adjoint specialiser check their handles before
+    touching a device."""
+    assert lib.sv_batch_set_executor(None, None, 1) == _lib.SV_ERR_ARG
+    assert lib.sv_adjoint_specialize(None, None) == _lib.SV_ERR_ARG
+    assert lib.sv_batch_pass_bytes(None, None) == _lib.SV_ERR_ARG
+
+
 @pytest.mark.parametrize("rc,exc", [(_lib.SV_ERR_ARG, ValueError), (_lib.SV_ERR_OOM, RuntimeError),
                                     (_lib.SV_ERR_UNSUPPORTED, NotImplementedError),
                                     (_lib.SV_ERR_TIMEOUT, TimeoutError), (_lib.SV_ERR_CUDA, RuntimeError)])
