@@ -196,6 +196,17 @@ def replicas_throughput(elapsed_ms: float, units_per_rank: float, device: str = 
     return elapsed_ms, ws * units_per_rank / (elapsed_ms / 1000.0)
 
 
+def _fp32_issue(arith_per_amp: float, n: int, ms: float) -> dict:
+    """The fused passes against their own bound: the plan's arithmetic lane instructions
+    (FFMA and FMUL, counted from its pass blocks by sv_program_arith_per_amplitude) over
+    the step's pass time, against the FP32 FMA rate a probe measured on this GPU type
+    (one lane instruction per FMA)."""
+    achieved = arith_per_amp * (1 << n) / (ms / 1000.0) / 1e12
+    peak = FP32_PEAK_TFLOPS / 2.0
+    return {"instructions_per_amplitude_per_step": arith_per_amp, "achieved": achieved, "peak": peak,
+            "unit": "T lane-instructions/s", "frac": achieved / peak, "peak_kind": "FP32 FMA rate of a probe"}
+
+
 def _time_program(torch, prog, backend, state, dcode, n, steps, stream):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -244,6 +255,9 @@ def run_engine(args):
     prog = backend.compile(circ, dtype, tile_bits=best[1], specialize=specialize)
     t_spec = time.perf_counter() - t_spec
     st = prog.stats()
+    # lane instructions (FFMA, FMUL) per amplitude of one step as planned: the bound of
+    # the fused complex64 passes is FP32 issue, not HBM
+    arith_per_amp = prog.arith_per_amplitude()
     state = backend.zero_state(n, dtype=dtype)
     stream = torch.cuda.current_stream()
 
@@ -391,7 +405,8 @@ def run_engine(args):
                          "traffic": _traffic_from_profiles(f"{kname}_{dtype}"), "peak_kind": peak_kind,
                          "kernel": kname, "algorithmic_bytes_per_launch": pass_bytes,
                          "avg_launch_ms": pass_ms, "dense_u3_equivalent_fp32_tflops": fp32_tflops,
-                         "dense_u3_equivalent_frac_of_fp32_probe_peak": fp32_tflops / FP32_PEAK_TFLOPS},
+                         "dense_u3_equivalent_frac_of_fp32_probe_peak": fp32_tflops / FP32_PEAK_TFLOPS,
+                         "fp32_issue": _fp32_issue(arith_per_amp, n, ms_step - zs_ms)},
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": param_bytes, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps,

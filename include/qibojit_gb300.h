@@ -277,6 +277,13 @@ int sv_program_specialize(sv_context* ctx, sv_program* prog);
  * the host copy of pass `pass`'s parameter block (what the pass kernel receives) and
  * its size, valid while the program lives. */
 int sv_program_pass_params(const sv_program* prog, int pass, const void** params, size_t* bytes);
+/* Arithmetic instructions per amplitude of one run of the program as planned (every
+ * pass touches every amplitude once): lane instructions of the pass kernels' register
+ * ops (FFMA and FMUL; FP32 for complex64, FP64 or their double-word expansion for
+ * complex128), with controlled ops counted for the amplitudes they select.  Times 2^n
+ * and divided by a run's duration it gives the rate to set against the FP32 issue peak:
+ * the bound of the fused complex64 passes.  No reference counterpart. */
+int sv_program_arith_per_amplitude(const sv_program* prog, double* out);
 /* Byte layout of a pass block for `dtype` (SV_C128 / SV_C64): 32 entries, in order
  * sizeof(block) and the offsets of n, kt, nphases, nops, ntiles, tile_pos, coef_goff,
  * phases, ops, coef; sizeof(phase), offsets of rb, op_begin, op_end; sizeof(op), offsets

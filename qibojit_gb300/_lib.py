@@ -28,7 +28,7 @@ EXPORTS = (
     "sv_context_set_stream", "sv_context_set_dense_mode", "sv_context_set_c128_arithmetic", "sv_sync", "sv_zero_state", "sv_apply_one_qubit", "sv_apply_two_qubit",
     "sv_apply_multi_qubit", "sv_collapse_state", "sv_probabilities", "sv_density_probabilities", "sv_axpby",
     "sv_measure_frequencies",
-    "sv_collapse_state_noalloc", "sv_sample_cdf", "sv_program_create", "sv_program_run", "sv_program_stats", "sv_program_specialize", "sv_program_pass_params", "sv_pass_layout",
+    "sv_collapse_state_noalloc", "sv_sample_cdf", "sv_program_create", "sv_program_run", "sv_program_stats", "sv_program_specialize", "sv_program_pass_params", "sv_program_arith_per_amplitude", "sv_pass_layout",
     "sv_program_destroy", "sv_inner_product", "sv_max_abs_diff", "sv_expectation_z",
     "sv_batch_create", "sv_batch_run", "sv_batch_specialize", "sv_batch_set_executor", "sv_batch_tfim_energy", "sv_batch_state", "sv_batch_stats", "sv_batch_pass_bytes",
     "sv_batch_destroy", "sv_adjoint_create", "sv_adjoint_update", "sv_adjoint_run", "sv_adjoint_specialize", "sv_adjoint_state",
@@ -75,6 +75,7 @@ _SIGNATURES = {
     "sv_program_specialize": ([_vp, _vp], _int),
     "sv_sample_cdf": ([_vp, _vp, _int, _int, _vp, ctypes.c_int64, _vp, _vp], _int),
     "sv_program_pass_params": ([_vp, _int, _vp, _vp], _int),
+    "sv_program_arith_per_amplitude": ([_vp, _vp], _int),
     "sv_pass_layout": ([_int, _vp, _int], _int),
     "sv_program_destroy": ([_vp], _int),
     "sv_inner_product": ([_vp, _vp, _int, _vp, _int, _int, _vp], _int),

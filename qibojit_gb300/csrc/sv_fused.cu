@@ -1510,6 +1510,64 @@ int sv_program_stats(const sv_program* prog, int* npasses, int* nunfused, int* n
   return SV_OK;
 }
 
+}  // extern "C"
+
+namespace sv {
+// arithmetic instructions per amplitude of one pass block under the pass kernels'
+// register ops (lane instructions, FMUL and FFMA alike): complex 2x2 8 per amplitude it
+// touches, real 2x2 4, pivoted real 2x2 2, complex 4x4 16, a diagonal or a diagonal
+// table one complex multiply (4); sign flips, X and SWAP are register moves (0).  Ops
+// under tile-level or thread-level controls count for the fraction of amplitudes their
+// masks select; a dense op's register-level mask selects pair (or quadruple) bases.
+template <typename T>
+static double pass_arith_per_amplitude(const PassParams<T>& p) {
+  double total = 0.0;
+  for (int q = 0; q < p.nops; q++) {
+    const FOp& f = p.ops[q];
+    double cost = 0.0;
+    // the register-level mask's bases: amplitudes for a diagonal, pair (quadruple) bases
+    // with the target bit(s) clear for a dense op
+    auto bases = [&](unsigned targets) {
+      int c = 0;
+      for (int j = 0; j < 16; j++)
+        if (!(j & targets) && ((f.jmask >> j) & 1u)) c++;
+      return (double)c;
+    };
+    switch (f.type) {
+      case FOP_D1RUN: cost = 8.0 * f.nrun; break;
+      case FOP_D1RUNR: cost = 4.0 * f.nrun; break;
+      case FOP_DIAGR: cost = 4.0; break;
+      case FOP_DENSE1: cost = 8.0 * bases(1u << f.u0) / 8.0; break;
+      case FOP_DENSE1R: cost = 4.0 * bases(1u << f.u0) / 8.0; break;
+      case FOP_DENSE1P: cost = 2.0 * bases(1u << f.u0) / 8.0; break;
+      case FOP_DENSE2: cost = 16.0 * bases((1u << f.u0) | (1u << f.u1)) / 4.0; break;
+      case FOP_DIAG: cost = 4.0 * bases(0) / 16.0; break;
+      default: cost = 0.0; break;  // sign flips, register swaps, gradient markers
+    }
+    if (f.type != FOP_D1RUN && f.type != FOP_D1RUNR && f.type != FOP_DIAGR) {
+      if (f.flags & FLAG_OMASK) cost /= (double)(1ull << __builtin_popcountll((unsigned long long)f.omask));
+      if (f.flags & FLAG_TMASK) cost /= (double)(1u << __builtin_popcount(f.tmask));
+    }
+    total += cost;
+  }
+  return total;
+}
+}  // namespace sv
+
+extern "C" {
+
+int sv_program_arith_per_amplitude(const sv_program* prog, double* out) {
+  if (!prog || !out) return set_error(SV_ERR_ARG, "null argument");
+  double total = 0.0;
+  for (int i = 0; i < prog->npasses; i++) {
+    const unsigned char* b = prog->passes.data() + (size_t)i * prog->pass_bytes;
+    total += prog->dtype == SV_C128 ? pass_arith_per_amplitude(*reinterpret_cast<const PassParams<c128>*>(b))
+                                    : pass_arith_per_amplitude(*reinterpret_cast<const PassParams<c64>*>(b));
+  }
+  *out = total;
+  return SV_OK;
+}
+
 int sv_program_pass_params(const sv_program* prog, int pass, const void** params, size_t* bytes) {
   if (!prog || !params || !bytes) return set_error(SV_ERR_ARG, "null argument");
   if (pass < 0 || pass >= prog->npasses) return set_error(SV_ERR_ARG, "pass %d out of range", pass);

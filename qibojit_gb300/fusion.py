@@ -144,6 +144,14 @@ class FusedProgram:
         return {"passes": a.value, "unfused": b.value, "fused_gates": c.value, "tile_bits": d.value,
                 "gates": self.ngates}
 
+    def arith_per_amplitude(self) -> float:
+        """Arithmetic lane instructions (FFMA and FMUL) per amplitude of one run as
+        planned (``sv_program_arith_per_amplitude``)."""
+        v = ctypes.c_double()
+        _lib.check(self._lib.sv_program_arith_per_amplitude(self._h, ctypes.byref(v)),
+                   "sv_program_arith_per_amplitude")
+        return v.value
+
     def param_bytes(self) -> int:
         """Bytes of the pass parameter blocks one run sends to the device with its
         launches (gate coefficients and the pass layout, as kernel parameters)."""

@@ -139,3 +139,55 @@ def test_qibo_fused_gates_are_planned_as_their_parts(lib):
     prog = FusedProgram(_HostContext(lib), circ.queue, n, "complex128", 8)
     x = random_state(n, 5)
     np.testing.assert_allclose(E.run_program(lib, prog._h, _lib.SV_C128, x), dense_reference(ref, x), atol=1e-12)
+
+
+def _tally(ps) -> float:
+    """The arithmetic model restated over a decoded pass block (lane instructions per
+    amplitude: complex 2x2 8, real 2x2 4, pivoted 2, complex 4x4 16, diagonal 4)."""
+    total = 0.0
+    for op in ps["ops"]:
+        t = op["type"]
+
+        def bases(targets):  # mask bits of pair (quadruple) bases: target bits clear
+            return sum(1 for j in range(16) if not (j & targets) and (op["jmask"] >> j) & 1)
+
+        one, two = 1 << op["u0"], (1 << op["u0"]) | (1 << op["u1"])
+        cost = {E.FOP_D1RUN: 8.0 * op["nrun"], E.FOP_D1RUNR: 4.0 * op["nrun"], E.FOP_DIAGR: 4.0,
+                E.FOP_DENSE1: bases(one), E.FOP_DENSE1R: 0.5 * bases(one), E.FOP_DENSE1P: 0.25 * bases(one),
+                E.FOP_DENSE2: 4.0 * bases(two), E.FOP_DIAG: 0.25 * bases(0)}.get(t, 0.0)
+        if t not in (E.FOP_D1RUN, E.FOP_D1RUNR, E.FOP_DIAGR):
+            if op["flags"] & E.FLAG_OMASK:
+                cost /= 2 ** bin(op["omask"]).count("1")
+            if op["flags"] & E.FLAG_TMASK:
+                cost /= 2 ** bin(op["tmask"]).count("1")
+        total += cost
+    return total
+
+
+@pytest.mark.parametrize("dt,refold", [("complex128", False), ("complex64", False), ("complex64", True)])
+@pytest.mark.parametrize("name", ["brickwork", "random"])
+def test_arithmetic_count_matches_the_pass_blocks(lib, dt, refold, name):
+    """sv_program_arith_per_amplitude against the same model evaluated on the decoded pass
+    blocks; the bench circuit's specialised plan (n=30, 2^13 tiles) needs 2,064 FP32
+    instructions per amplitude per step (582 pivoted real 2x2s, 195 diagonal tables, 30
+    thread-bit diagonals), the count ncu's FFMA + FMUL figures confirm per pass."""
+    n = 30 if name == "brickwork" else 12
+    circ = circuits.brickwork(n, 20, 1234) if name == "brickwork" else random_circuit(n, 200, 9, families=FUSABLE)
+    tile_bits = 13 if (name == "brickwork" and dt == "complex64") else 0
+    rc, h, ctx, _ = _create(lib, circ, dt, tile_bits)
+    assert rc == _lib.SV_OK, _lib.last_error()
+    try:
+        if refold:
+            rc = lib.sv_program_specialize(ctypes.addressof(ctx), h)
+            if rc == _lib.SV_ERR_UNSUPPORTED:
+                pytest.skip(_lib.last_error())
+        got = ctypes.c_double()
+        _lib.check(lib.sv_program_arith_per_amplitude(h, ctypes.byref(got)))
+        passes = ctypes.c_int()
+        _lib.check(lib.sv_program_stats(h, ctypes.byref(passes), None, None, None))
+        want = sum(_tally(E.read_pass(lib, h, i, _lib.DTYPE_CODES[dt])) for i in range(passes.value))
+        assert got.value == pytest.approx(want, rel=1e-12)
+        if name == "brickwork" and dt == "complex64" and refold:
+            assert got.value == pytest.approx(2064.0)
+    finally:
+        lib.sv_program_destroy(h)
