@@ -201,10 +201,14 @@ def _fp32_issue(arith_per_amp: float, n: int, ms: float) -> dict:
     (FFMA and FMUL, counted from its pass blocks by sv_program_arith_per_amplitude) over
     the step's pass time, against the FP32 FMA rate a probe measured on this GPU type
     (one lane instruction per FMA)."""
-    achieved = arith_per_amp * (1 << n) / (ms / 1000.0) / 1e12
+    return _fp32_issue_total(arith_per_amp * (1 << n), ms) | {"instructions_per_amplitude_per_step": arith_per_amp}
+
+
+def _fp32_issue_total(instructions: float, ms: float) -> dict:
+    achieved = instructions / (ms / 1000.0) / 1e12
     peak = FP32_PEAK_TFLOPS / 2.0
-    return {"instructions_per_amplitude_per_step": arith_per_amp, "achieved": achieved, "peak": peak,
-            "unit": "T lane-instructions/s", "frac": achieved / peak, "peak_kind": "FP32 FMA rate of a probe"}
+    return {"instructions": instructions, "achieved": achieved, "peak": peak, "unit": "T lane-instructions/s",
+            "frac": achieved / peak, "peak_kind": "FP32 FMA rate of a probe"}
 
 
 def _time_program(torch, prog, backend, state, dcode, n, steps, stream):
@@ -666,6 +670,8 @@ def _extra_workloads(torch, backend, stream, args):
                   "persistent_max_abs_energy_diff": float(np.abs(e_persist - en).max()), "stats": st,
                   # every circuit's plan passes, each one read and one write of its state
                   "roofline": _frac(st["pass_bytes"], ms)}
+        if dt == "complex64":  # the passes' arithmetic against the FP32 issue bound
+            vq[dt]["fp32_issue"] = _fp32_issue_total(st["arith_instructions"], ms)
         vq[dt]["energies_head"] = [float(v) for v in en[:3]]
         batches[dt] = (bat, en)
     (b64, e64), (b128, e128) = batches["complex64"], batches["complex128"]

@@ -327,6 +327,9 @@ int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_
 /* Algorithmic HBM bytes of one run's gate passes: for every circuit, its plan's pass
  * count times one read and one write of its state (the |0...0> fill excluded). */
 int sv_batch_pass_bytes(const sv_batch* b, double* bytes);
+/* Arithmetic lane instructions of one run's gate passes: for every circuit, its plan's
+ * sv_program_arith_per_amplitude times its 2^n amplitudes. */
+int sv_batch_arith(const sv_batch* b, double* instructions);
 int sv_batch_destroy(sv_batch* b);
 
 /* ---------------------------------------------------------- adjoint gradients */

@@ -30,7 +30,7 @@ EXPORTS = (
     "sv_measure_frequencies",
     "sv_collapse_state_noalloc", "sv_sample_cdf", "sv_program_create", "sv_program_run", "sv_program_stats", "sv_program_specialize", "sv_program_pass_params", "sv_program_arith_per_amplitude", "sv_pass_layout",
     "sv_program_destroy", "sv_inner_product", "sv_max_abs_diff", "sv_expectation_z",
-    "sv_batch_create", "sv_batch_run", "sv_batch_specialize", "sv_batch_set_executor", "sv_batch_tfim_energy", "sv_batch_state", "sv_batch_stats", "sv_batch_pass_bytes",
+    "sv_batch_create", "sv_batch_run", "sv_batch_specialize", "sv_batch_set_executor", "sv_batch_tfim_energy", "sv_batch_state", "sv_batch_stats", "sv_batch_pass_bytes", "sv_batch_arith",
     "sv_batch_destroy", "sv_adjoint_create", "sv_adjoint_update", "sv_adjoint_run", "sv_adjoint_specialize", "sv_adjoint_state",
     "sv_adjoint_destroy",
 )
@@ -89,6 +89,7 @@ _SIGNATURES = {
     "sv_batch_state": ([_vp, _int, ctypes.POINTER(_vp), ctypes.POINTER(_int)], _int),
     "sv_batch_stats": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_size_t)], _int),
     "sv_batch_pass_bytes": ([_vp, _vp], _int),
+    "sv_batch_arith": ([_vp, _vp], _int),
     "sv_batch_destroy": ([_vp], _int),
     "sv_adjoint_create": ([_vp, _int, _int, _int, _vp, _int, _vp, _vp, _int, _vp, _int, _int, ctypes.POINTER(_vp)],
                           _int),

@@ -140,9 +140,11 @@ class BatchedCircuits:
     def stats(self) -> dict:
         g, p, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
         _lib.check(self.lib.sv_batch_stats(self._h, ctypes.byref(g), ctypes.byref(p), ctypes.byref(b)))
-        pb = ctypes.c_double()
+        pb, ar = ctypes.c_double(), ctypes.c_double()
         _lib.check(self.lib.sv_batch_pass_bytes(self._h, ctypes.byref(pb)))
-        return {"groups": g.value, "passes": p.value, "state_bytes": b.value, "pass_bytes": pb.value}
+        _lib.check(self.lib.sv_batch_arith(self._h, ctypes.byref(ar)))
+        return {"groups": g.value, "passes": p.value, "state_bytes": b.value, "pass_bytes": pb.value,
+                "arith_instructions": ar.value}
 
     def run(self) -> None:
         _lib.check(self.lib.sv_batch_run(self.ctx.handle, self._h), "sv_batch_run")

@@ -1552,19 +1552,22 @@ static double pass_arith_per_amplitude(const PassParams<T>& p) {
   }
   return total;
 }
-}  // namespace sv
-
-extern "C" {
-
-int sv_program_arith_per_amplitude(const sv_program* prog, double* out) {
-  if (!prog || !out) return set_error(SV_ERR_ARG, "null argument");
+static double program_arith_per_amplitude(const sv_program* prog) {
   double total = 0.0;
   for (int i = 0; i < prog->npasses; i++) {
     const unsigned char* b = prog->passes.data() + (size_t)i * prog->pass_bytes;
     total += prog->dtype == SV_C128 ? pass_arith_per_amplitude(*reinterpret_cast<const PassParams<c128>*>(b))
                                     : pass_arith_per_amplitude(*reinterpret_cast<const PassParams<c64>*>(b));
   }
-  *out = total;
+  return total;
+}
+}  // namespace sv
+
+extern "C" {
+
+int sv_program_arith_per_amplitude(const sv_program* prog, double* out) {
+  if (!prog || !out) return set_error(SV_ERR_ARG, "null argument");
+  *out = program_arith_per_amplitude(prog);
   return SV_OK;
 }
 
@@ -2381,6 +2384,17 @@ int sv_batch_stats(const sv_batch* b, int* ngroups, int* npasses, size_t* state_
   if (ngroups) *ngroups = (int)b->groups.size();
   if (npasses) *npasses = np;
   if (state_bytes) *state_bytes = b->total * dtype_size(b->dtype);
+  return SV_OK;
+}
+
+int sv_batch_arith(const sv_batch* b, double* instructions) {
+  if (!b || !instructions) return set_error(SV_ERR_ARG, "bad batch query");
+  double total = 0.0;
+  for (auto& g : b->groups) {
+    const double per_amp = program_arith_per_amplitude(g.prog);
+    for (int c : g.circuits) total += per_amp * (double)((int64_t)1 << b->nq[c]);
+  }
+  *instructions = total;
   return SV_OK;
 }
 

@@ -75,6 +75,8 @@ def test_null_handles_are_rejected_by_batch_and_adjoint_entry_points(lib):
     assert lib.sv_batch_set_executor(None, None, 1) == _lib.SV_ERR_ARG
     assert lib.sv_adjoint_specialize(None, None) == _lib.SV_ERR_ARG
     assert lib.sv_batch_pass_bytes(None, None) == _lib.SV_ERR_ARG
+    assert lib.sv_batch_arith(None, None) == _lib.SV_ERR_ARG
+    assert lib.sv_program_arith_per_amplitude(None, None) == _lib.SV_ERR_ARG
 
 
 @pytest.mark.parametrize("rc,exc", [(_lib.SV_ERR_ARG, ValueError), (_lib.SV_ERR_OOM, RuntimeError),
